@@ -1,0 +1,172 @@
+/* pcf.h -- C ABI of the GB300 option-pricing engine (libpcf.so).
+ *
+ * Drop-in boundary for the pricing functions of moledoc/parcompfin. The
+ * reference exposes one `double method(...)` C++ function per pricing method,
+ * called from each program's main() between two clock reads; every entry
+ * point below replaces one of them (file:line cited on each) and keeps its
+ * parameters (S0, E, r, sigma, T, N, M, payoff_fun, assets, rho) in the same
+ * order and meaning. payoff_fun is +1 for a call and -1 for a put, as in
+ * include/common.h:56-60.
+ *
+ * Conventions:
+ *   - every function returns a status (PCF_OK or a negative PCF_E* code);
+ *     no C++ exception crosses the ABI. The reference throws
+ *     std::invalid_argument for a bad payoff (src/mc_eur.cpp:42), an odd path
+ *     count for the LSM paths (include/common.h:180) and a singular regression
+ *     (include/common.h:115-117); those map to PCF_EINVAL / PCF_ESINGULAR.
+ *   - results are written to caller-owned host memory; the library owns all
+ *     device memory through a context.
+ *   - ctx may be NULL: the calling thread's default context on device 0 is
+ *     created on first use.
+ *   - one context serves one host thread at a time (or serialise externally).
+ *   - the Monte Carlo paths draw from a counter-based Philox4x32-10 stream
+ *     keyed by `seed`, so a call is reproducible; the reference reseeds from
+ *     time() (src/mc_eur.cpp:19) and is not.
+ */
+#ifndef PCF_H_
+#define PCF_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PCF_API __attribute__((visibility("default")))
+#else
+#define PCF_API
+#endif
+
+#define PCF_OK 0
+#define PCF_EINVAL (-1)     /* bad parameter (payoff_fun not +/-1, N < 1, ...) */
+#define PCF_ENOMEM (-2)     /* device or pinned allocation failed / over budget */
+#define PCF_ESINGULAR (-3)  /* LSM normal equations with determinant <= 0 */
+#define PCF_ETIMEOUT (-4)   /* a bounded device wait gave up */
+#define PCF_ECUDA (-5)      /* CUDA runtime error */
+#define PCF_ENODEV (-6)     /* no CUDA device */
+
+typedef struct pcf_ctx pcf_ctx;
+
+/* Result of a Monte Carlo price. `price`/`std_error` are the estimate that
+ * was asked for: the plain discounted mean (use_cv = 0, what the reference
+ * returns) or the control-variate estimate (use_cv = 1). `sums` are the raw
+ * moment sums {sum y, sum y^2, sum g, sum g^2, sum y*g} over n_paths paths,
+ * y the undiscounted payoff (the discounted cash flow for mc_amer) and g the
+ * method's control variate. */
+typedef struct pcf_mc_result {
+  double price;
+  double std_error;
+  double price_plain;
+  double std_error_plain;
+  double price_cv;        /* NaN when use_cv = 0 */
+  double std_error_cv;    /* NaN when use_cv = 0 */
+  double cv_beta;
+  double cv_mean;         /* exact E[g] */
+  double discount;        /* factor applied to the mean of y */
+  double sums[5];
+  long long n_paths;
+} pcf_mc_result;
+
+/* Library version string. */
+PCF_API const char* pcf_version(void);
+/* Message for a status code. */
+PCF_API const char* pcf_strerror(int status);
+/* Details of the last error on this thread (empty if none). */
+PCF_API const char* pcf_last_error(void);
+
+/* Context: a CUDA stream plus device and pinned scratch that persists across
+ * calls. Replaces nothing in the reference (it has no device state). */
+PCF_API int pcf_ctx_create(int device, pcf_ctx** out);
+PCF_API int pcf_ctx_destroy(pcf_ctx* ctx);
+/* The context's cudaStream_t, for callers that time or order work on it. */
+PCF_API void* pcf_ctx_stream(pcf_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+PCF_API long long pcf_ctx_launch_count(pcf_ctx* ctx);
+
+/* European option, single-step GBM Monte Carlo.
+ * Replaces double mc_eur(S0,E,r,sigma,T,N,payoff_fun), src/mc_eur.cpp:5-27
+ * (OpenMP: src/mc_eur_omp.cpp:5-30). Control variate g = S_T. */
+PCF_API int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+               long long N, int payoff_fun, unsigned long long seed, int use_cv,
+               pcf_mc_result* out);
+
+/* Fixed-strike arithmetic-average Asian option, M monitoring steps.
+ * Replaces double mc_asia(S0,E,r,sigma,T,N,M,payoff_fun), src/mc_asia.cpp:5-40
+ * (OpenMP: src/mc_asia_omp.cpp:5-48). mode 0 reproduces the reference's
+ * running sum I += S (1 + r dt/2 + sigma dB/2) (src/mc_asia.cpp:33);
+ * mode 1 averages S_1..S_M. Control variate: the geometric average payoff. */
+PCF_API int pcf_mc_asia(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+                long long N, int M, int payoff_fun, int mode, unsigned long long seed,
+                int use_cv, pcf_mc_result* out);
+
+/* Equal-weight basket of `assets` assets with common S0 and sigma and
+ * equicorrelation rho, single step.
+ * Replaces double mc_eur(S0,E,r,sigma,T,N,payoff_fun,assets,rho),
+ * src/mc_eur_multi.cpp:6-35 with mvnorm() of include/mvn.h:42-82. Like the
+ * reference, the correlated draws are not scaled by sqrt(T) (include/mvn.h:55-60,
+ * src/mc_eur_multi.cpp:30). Control variate: the geometric basket payoff. */
+PCF_API int pcf_mc_eur_multi(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+                     long long N, int payoff_fun, int assets, double rho,
+                     unsigned long long seed, int use_cv, pcf_mc_result* out);
+
+/* General basket: per-asset S0[d] and sigma[d], correlation corr[d*d]
+ * (row-major, symmetric positive semi-definite), 1 <= d <= 64. The factor is
+ * Cholesky, or the eigen square root when Cholesky fails (include/mvn.h:63-76).
+ * scale_by_sqrt_T = 1 scales the draws by sqrt(T) (a GBM basket); 0 keeps the
+ * reference's unscaled draws. Extension of src/mc_eur_multi.cpp:6-35. */
+PCF_API int pcf_mc_basket(pcf_ctx* ctx, int d, const double* S0, const double* sigma,
+                  const double* corr, double r, double T, double E, long long N,
+                  int payoff_fun, int scale_by_sqrt_T, unsigned long long seed, int use_cv,
+                  pcf_mc_result* out);
+
+/* ---- Batched pricing -----------------------------------------------------
+ * The reference prices one contract per process run (one main() per price).
+ * A batch prices many contracts of mixed methods, uneven path and step
+ * counts in one persistent launch per method, whose blocks pull work items
+ * from a device queue. Each request draws from its own Philox stream
+ * (seed, stream), so its result does not depend on what else is in the batch
+ * beyond FP64 summation order. */
+#define PCF_METHOD_EUR 0
+#define PCF_METHOD_ASIA 1
+#define PCF_METHOD_BASKET 2
+#define PCF_METHOD_AMER 3
+
+typedef struct pcf_mc_request {
+  int method;             /* PCF_METHOD_* */
+  int payoff_fun;         /* +1 call, -1 put */
+  double S0, E, r, sigma, T;
+  long long N;            /* paths */
+  int M;                  /* Asian steps, American exercise dates */
+  int mode;               /* Asian averaging mode; American: 1 = reference exercise rule */
+  int use_cv;             /* report the control-variate estimate as `price` */
+  int assets;             /* basket size d (1..64) */
+  double rho;             /* basket equicorrelation, used when corr == NULL */
+  const double* basket_S0;    /* [d] or NULL (all S0) */
+  const double* basket_sigma; /* [d] or NULL (all sigma) */
+  const double* corr;         /* [d*d] row-major or NULL (equicorrelation rho) */
+  int scale_by_sqrt_T;    /* basket: 1 = GBM draws scaled by sqrt(T) */
+  unsigned long long seed;
+  unsigned int stream;    /* Philox stream id (e.g. the request id) */
+} pcf_mc_request;
+
+/* A plan holds a batch's contract tables and results on the device, so it
+ * can be launched repeatedly (or captured in a CUDA graph) with no host
+ * traffic. */
+typedef struct pcf_plan pcf_plan;
+PCF_API int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** out);
+/* Enqueue the plan's kernels on the context stream; returns without waiting. */
+PCF_API int pcf_plan_launch(pcf_plan* plan);
+/* Wait for the plan's last launch and fill results[n]. */
+PCF_API int pcf_plan_results(pcf_plan* plan, pcf_mc_result* results);
+/* Kernels one pcf_plan_launch enqueues. */
+PCF_API int pcf_plan_kernel_count(const pcf_plan* plan);
+PCF_API int pcf_plan_destroy(pcf_plan* plan);
+
+/* Price n requests in one call: create, launch, read back, destroy. */
+PCF_API int pcf_price_batch(pcf_ctx* ctx, int n, const pcf_mc_request* reqs,
+                            pcf_mc_result* results);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PCF_H_ */

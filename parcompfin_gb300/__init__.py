@@ -1,0 +1,21 @@
+"""GB300-native pricing engine for the hot path of moledoc/parcompfin.
+
+The pricing functions run hand-written sm_103a CUDA kernels in libpcf.so
+through its C ABI (include/pcf.h); see api.py for the functions that mirror
+the reference's.
+"""
+from .api import (  # noqa: F401
+    Context,
+    Plan,
+    price_batch,
+    request,
+    mc_asia,
+    mc_asia_result,
+    mc_basket_result,
+    mc_eur,
+    mc_eur_multi,
+    mc_eur_multi_result,
+    mc_eur_result,
+    payoff_code,
+)
+from ._lib import McResult, PcfError, load  # noqa: F401

@@ -1,0 +1,218 @@
+"""Python mirror of the reference's pricing functions, priced on the GPU.
+
+Each function keeps the name, argument order and meaning of the reference
+function it replaces and returns the price as a float, as the reference
+does:
+
+    mc_eur(S0, E, r, sigma, T, N, payoff_fun)            src/mc_eur.cpp:5-27
+    mc_eur_multi(S0, E, r, sigma, T, N, payoff_fun, assets, rho)
+                                                          src/mc_eur_multi.cpp:6-35
+    mc_asia(S0, E, r, sigma, T, N, M, payoff_fun)        src/mc_asia.cpp:5-40
+
+payoff_fun is +1/-1 (the reference's encoding, include/common.h:56-60) or
+the strings "call"/"put" its command lines accept (src/mc_eur.cpp:39-42).
+Anything else raises ValueError("Unknown payoff function"), like the
+reference's std::invalid_argument. Keyword-only extras (seed, use_cv, mode,
+ctx) select what the reference fixes: the reference seeds from time(), and
+here the Philox seed is explicit and defaults to 0. The *_result variants
+return the full McResult (price, standard error, control-variate estimate,
+raw moment sums).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _lib
+
+
+def payoff_code(payoff_fun) -> int:
+    if isinstance(payoff_fun, str):
+        if payoff_fun == "call":
+            return 1
+        if payoff_fun == "put":
+            return -1
+        raise ValueError("Unknown payoff function")
+    if payoff_fun in (1, 1.0):
+        return 1
+    if payoff_fun in (-1, -1.0):
+        return -1
+    raise ValueError("Unknown payoff function")
+
+
+class Context:
+    """A libpcf context: one CUDA stream plus resident device scratch."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib.load()
+        h = C.c_void_p()
+        _lib.check(lib.pcf_ctx_create(int(device), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return _lib.load().pcf_ctx_stream(self._h) or 0
+
+    @property
+    def launches(self) -> int:
+        return int(_lib.load().pcf_ctx_launch_count(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            _lib.load().pcf_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def _h(ctx):
+    return None if ctx is None else ctx.handle
+
+
+def mc_eur_result(S0, E, r, sigma, T, N, payoff_fun, *, seed=0, use_cv=False, ctx=None):
+    lib = _lib.load()
+    out = _lib.McResult()
+    _lib.check(lib.pcf_mc_eur(_h(ctx), S0, E, r, sigma, T, int(N), payoff_code(payoff_fun),
+                              int(seed), int(bool(use_cv)), C.byref(out)))
+    return out
+
+
+def mc_eur(S0, E, r, sigma, T, N, payoff_fun, *, seed=0, use_cv=False, ctx=None) -> float:
+    return mc_eur_result(S0, E, r, sigma, T, N, payoff_fun, seed=seed, use_cv=use_cv,
+                         ctx=ctx).price
+
+
+def mc_asia_result(S0, E, r, sigma, T, N, M, payoff_fun, *, mode=0, seed=0, use_cv=False,
+                   ctx=None):
+    lib = _lib.load()
+    out = _lib.McResult()
+    _lib.check(lib.pcf_mc_asia(_h(ctx), S0, E, r, sigma, T, int(N), int(M),
+                               payoff_code(payoff_fun), int(mode), int(seed),
+                               int(bool(use_cv)), C.byref(out)))
+    return out
+
+
+def mc_asia(S0, E, r, sigma, T, N, M, payoff_fun, *, mode=0, seed=0, use_cv=False,
+            ctx=None) -> float:
+    return mc_asia_result(S0, E, r, sigma, T, N, M, payoff_fun, mode=mode, seed=seed,
+                          use_cv=use_cv, ctx=ctx).price
+
+
+def mc_eur_multi_result(S0, E, r, sigma, T, N, payoff_fun, assets, rho, *, seed=0,
+                        use_cv=False, ctx=None):
+    lib = _lib.load()
+    out = _lib.McResult()
+    _lib.check(lib.pcf_mc_eur_multi(_h(ctx), S0, E, r, sigma, T, int(N),
+                                    payoff_code(payoff_fun), int(assets), float(rho),
+                                    int(seed), int(bool(use_cv)), C.byref(out)))
+    return out
+
+
+def mc_eur_multi(S0, E, r, sigma, T, N, payoff_fun, assets, rho, *, seed=0, use_cv=False,
+                 ctx=None) -> float:
+    return mc_eur_multi_result(S0, E, r, sigma, T, N, payoff_fun, assets, rho, seed=seed,
+                               use_cv=use_cv, ctx=ctx).price
+
+
+METHODS = {"eur": _lib.METHOD_EUR, "asia": _lib.METHOD_ASIA, "basket": _lib.METHOD_BASKET,
+           "amer": _lib.METHOD_AMER}
+
+
+def request(method, S0, E, r, sigma, T, N, payoff_fun, *, M=0, mode=0, use_cv=False,
+            assets=0, rho=0.0, basket_S0=None, basket_sigma=None, corr=None,
+            scale_by_sqrt_T=True, seed=0, stream=0) -> dict:
+    """One pricing request for price_batch / Plan (a dict of pcf_mc_request fields)."""
+    return dict(method=METHODS[method] if isinstance(method, str) else int(method),
+                payoff_fun=payoff_code(payoff_fun), S0=float(S0), E=float(E), r=float(r),
+                sigma=float(sigma), T=float(T), N=int(N), M=int(M), mode=int(mode),
+                use_cv=int(bool(use_cv)), assets=int(assets), rho=float(rho),
+                basket_S0=basket_S0, basket_sigma=basket_sigma, corr=corr,
+                scale_by_sqrt_T=int(bool(scale_by_sqrt_T)), seed=int(seed), stream=int(stream))
+
+
+def _pack(reqs):
+    arr = (_lib.McRequest * len(reqs))()
+    keep = []
+    for i, q in enumerate(reqs):
+        x = arr[i]
+        for k, v in q.items():
+            if k in ("basket_S0", "basket_sigma", "corr"):
+                if v is None:
+                    continue
+                flat = [float(t) for row in v for t in row] if hasattr(v[0], "__len__") else \
+                    [float(t) for t in v]
+                buf = (C.c_double * len(flat))(*flat)
+                keep.append(buf)
+                setattr(x, k, C.cast(buf, C.POINTER(C.c_double)))
+            else:
+                setattr(x, k, v)
+    return arr, keep
+
+
+class Plan:
+    """Device-resident batch: upload once, launch many times (graph-capturable)."""
+
+    def __init__(self, reqs, ctx=None):
+        lib = _lib.load()
+        arr, keep = _pack(reqs)
+        h = C.c_void_p()
+        _lib.check(lib.pcf_plan_create(_h(ctx), len(reqs), arr, C.byref(h)))
+        self._h, self.n = h, len(reqs)
+
+    def launch(self):
+        _lib.check(_lib.load().pcf_plan_launch(self._h))
+
+    def results(self):
+        out = (_lib.McResult * self.n)()
+        _lib.check(_lib.load().pcf_plan_results(self._h, out))
+        return list(out)
+
+    @property
+    def kernel_count(self) -> int:
+        return int(_lib.load().pcf_plan_kernel_count(self._h))
+
+    def close(self):
+        if self._h:
+            _lib.load().pcf_plan_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def price_batch(reqs, ctx=None):
+    """Price a list of request() dicts in one call; returns McResult per request."""
+    lib = _lib.load()
+    arr, keep = _pack(reqs)
+    out = (_lib.McResult * len(reqs))()
+    _lib.check(lib.pcf_price_batch(_h(ctx), len(reqs), arr, out))
+    return list(out)
+
+
+def mc_basket_result(S0s, sigmas, corr, r, T, E, N, payoff_fun, *, scale_by_sqrt_T=True,
+                     seed=0, use_cv=False, ctx=None):
+    """General basket: per-asset spots and vols, full correlation matrix."""
+    lib = _lib.load()
+    d = len(S0s)
+    flat = [float(x) for row in corr for x in row] if hasattr(corr[0], "__len__") else \
+        [float(x) for x in corr]
+    if len(sigmas) != d or len(flat) != d * d:
+        raise ValueError("S0s, sigmas and corr sizes do not match")
+    A = C.c_double * d
+    out = _lib.McResult()
+    _lib.check(lib.pcf_mc_basket(_h(ctx), d, A(*map(float, S0s)), A(*map(float, sigmas)),
+                                 (C.c_double * (d * d))(*flat), r, T, E, int(N),
+                                 payoff_code(payoff_fun), int(bool(scale_by_sqrt_T)),
+                                 int(seed), int(bool(use_cv)), C.byref(out)))
+    return out

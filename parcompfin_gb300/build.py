@@ -1,0 +1,94 @@
+"""In-tree build of the engine's shared library (libpcf.so) with nvcc.
+
+Every CUDA translation unit is compiled for sm_103a only, in parallel, and
+linked with the host C++ units into parcompfin_gb300/_lib/libpcf.so. The
+library is loaded from the source tree (never installed), so the extension
+that tests and benchmarks use is the one built here.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+OUT_DIR = os.path.join(PKG, "_lib")
+BUILD_DIR = os.path.join(PKG, "_build")
+LIB = os.path.join(OUT_DIR, "libpcf.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+           "-Xcompiler", "-fvisibility=hidden"]
+
+# (source, extra flags). The binomial unit must not contract a*b+c into FMA:
+# it reproduces the reference's FP64 rounding sequence term by term.
+SOURCES = [
+    ("mc_kernels.cu", []),
+    ("lsm.cu", []),
+    ("binom.cu", ["-fmad=false"]),
+    ("pcf_api.cpp", []),
+    ("pcf_batch.cpp", []),
+    ("pcf_math.cpp", []),
+]
+
+
+def _nvcc() -> str:
+    for c in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libpcf")
+
+
+def _sources():
+    return [(s, f) for s, f in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    for name in os.listdir(CSRC):
+        if os.path.getmtime(os.path.join(CSRC, name)) > t:
+            return True
+    inc = os.path.join(os.path.dirname(PKG), "include", "pcf.h")
+    return os.path.exists(inc) and os.path.getmtime(inc) > t
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile libpcf.so if any source is newer than it; return its path."""
+    if not force and not _stale():
+        return LIB
+    nvcc = _nvcc()
+    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(BUILD_DIR, exist_ok=True)
+
+    def compile_one(item):
+        src, extra = item
+        obj = os.path.join(BUILD_DIR, src + ".o")
+        cmd = [nvcc, *ARCH, *NVFLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+        if src.endswith(".cpp"):
+            cmd = [nvcc, "-x", "cu", *ARCH, *NVFLAGS, *extra, "-c", os.path.join(CSRC, src),
+                   "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
+        if verbose:
+            sys.stderr.write(r.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        objs = list(ex.map(compile_one, _sources()))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

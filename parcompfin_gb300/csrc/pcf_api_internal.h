@@ -1,0 +1,55 @@
+// Host-side internals shared by the C-ABI translation units: the context
+// object and the helpers that validate, allocate and report errors.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/pcf.h"
+#include "pcf_internal.h"
+
+struct pcf_ctx {
+  int device = 0;
+  int sm_count = 1;
+  cudaStream_t stream = nullptr;
+  // Scratch arena for launch parameters, partial sums and results; grown on
+  // demand and reused by every call on this context.
+  void* d_buf = nullptr;
+  size_t d_cap = 0;
+  void* h_buf = nullptr;  // pinned staging
+  size_t h_cap = 0;
+  // Longstaff-Schwartz path matrix and per-path state, kept resident.
+  void* d_paths = nullptr;
+  size_t paths_cap = 0;
+  // log((double)n) table for the reference-order binomial sum.
+  double* d_logtab = nullptr;
+  int logtab_n = 0;
+  // Upper bound on device bytes this context may hold (0 = unlimited).
+  size_t budget_bytes = 0;
+  long long launches = 0;
+};
+
+namespace pcf {
+
+int set_error(int status, const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+int ctx_ensure(pcf_ctx* c, size_t dev_bytes, size_t host_bytes);
+pcf_ctx* resolve_ctx(pcf_ctx* ctx, int* status);
+void ctx_release_extras(pcf_ctx* c);
+int check_common(double S0, double E, double r, double sigma, double T, long long N, int pf);
+void fill_result(const double* s, long long n, double mu_g, double disc, bool use_cv,
+                 pcf_mc_result* out);
+
+McContract make_eur(const pcf_ctx* c, double S0, double E, double r, double sigma, double T,
+                    long long N, int pf, unsigned long long seed, uint32_t stream);
+McContract make_asia(double S0, double E, double r, double sigma, double T, long long N, int M,
+                     int pf, int mode, unsigned long long seed, uint32_t stream);
+double asia_cv_mean(double S0, double E, double r, double sigma, double T, int M, int pf,
+                    int mode);
+int make_basket(int d, const double* S0, const double* sig, const double* corr, double r,
+                double T, double E, long long N, int pf, double ts, unsigned long long seed,
+                uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g);
+
+}  // namespace pcf

@@ -1,0 +1,293 @@
+// Batched pricing plans (pcf_plan_*, pcf_price_batch in include/pcf.h).
+//
+// A plan groups requests by method and uploads, once, each group's contract
+// table, the item prefix table and the basket factors. A launch is then one
+// memset (the groups' completion tickets and work-queue heads) plus one
+// persistent kernel per method group, with no host traffic, so a plan can be
+// replayed or captured in a CUDA graph. Results are read back in one copy.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "pcf_api_internal.h"
+#include "pcf_math.h"
+
+using namespace pcf;
+
+namespace {
+
+struct Group {
+  McMethod method;
+  int max_d = 0;
+  std::vector<int> req;           // request index of each contract (queue order)
+  std::vector<McContract> cs;
+  std::vector<float> fb;
+  std::vector<int> start;         // item prefix, size C+1
+  McLaunch L{};
+  int grid = 0;
+};
+
+size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct pcf_plan {
+  pcf_ctx* ctx = nullptr;
+  int n = 0;
+  std::vector<Group> groups;
+  std::vector<long long> npaths;
+  std::vector<double> mu_g, disc;
+  std::vector<int> use_cv;
+  std::vector<int> out_slot;  // request -> row of the device out table
+  void* d_mem = nullptr;
+  double* h_out = nullptr;
+  unsigned* d_tickets = nullptr;
+  size_t tickets_bytes = 0;
+  double* d_out = nullptr;
+};
+
+static int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContract& k,
+                         std::vector<float>& fb, double& mu_g, double& disc) {
+  int st = check_common(q.method == PCF_METHOD_BASKET && q.basket_S0 ? 1.0 : q.S0, q.E, q.r,
+                        q.sigma, q.T, q.N, q.payoff_fun);
+  if (st) return set_error(st, "request %d: %s", idx, pcf_last_error());
+  disc = exp(-q.r * q.T);
+  switch (q.method) {
+    case PCF_METHOD_EUR:
+      if (q.N > (1LL << 46)) return set_error(PCF_EINVAL, "request %d: N too large", idx);
+      k = make_eur(c, q.S0, q.E, q.r, q.sigma, q.T, q.N, q.payoff_fun, q.seed, q.stream);
+      mu_g = q.S0 * exp(q.r * q.T);
+      return PCF_OK;
+    case PCF_METHOD_ASIA:
+      if (q.M < 1 || q.M > (1 << 20) || (q.mode != 0 && q.mode != 1) || q.N > (1LL << 38))
+        return set_error(PCF_EINVAL, "request %d: bad Asian M/mode/N", idx);
+      k = make_asia(q.S0, q.E, q.r, q.sigma, q.T, q.N, q.M, q.payoff_fun, q.mode, q.seed,
+                    q.stream);
+      mu_g = asia_cv_mean(q.S0, q.E, q.r, q.sigma, q.T, q.M, q.payoff_fun, q.mode);
+      return PCF_OK;
+    case PCF_METHOD_BASKET: {
+      const int d = q.assets;
+      if (d < 1 || d > 64 || q.N > (1LL << 38))
+        return set_error(PCF_EINVAL, "request %d: basket size must be in [1, 64]", idx);
+      std::vector<double> s0((size_t)d), sg((size_t)d), cor((size_t)d * d);
+      for (int a = 0; a < d; ++a) {
+        s0[a] = q.basket_S0 ? q.basket_S0[a] : q.S0;
+        sg[a] = q.basket_sigma ? q.basket_sigma[a] : q.sigma;
+      }
+      if (q.corr) {
+        memcpy(cor.data(), q.corr, sizeof(double) * d * d);
+      } else {
+        if (!(q.rho >= -1 && q.rho <= 1))
+          return set_error(PCF_EINVAL, "request %d: rho must be in [-1, 1]", idx);
+        for (int i = 0; i < d * d; ++i) cor[i] = q.rho;
+        for (int a = 0; a < d; ++a) cor[(size_t)a * d + a] = 1.0;
+      }
+      st = make_basket(d, s0.data(), sg.data(), cor.data(), q.r, q.T, q.E, q.N, q.payoff_fun,
+                       q.scale_by_sqrt_T ? sqrt(q.T) : 1.0, q.seed, q.stream, fb, k, mu_g);
+      if (st) return set_error(st, "request %d: %s", idx, pcf_last_error());
+      return PCF_OK;
+    }
+    default:
+      return set_error(PCF_EINVAL, "request %d: method %d not supported in a batch", idx,
+                       q.method);
+  }
+}
+
+extern "C" {
+
+int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** out) {
+  if (!out || (n > 0 && !reqs) || n < 0) return set_error(PCF_EINVAL, "bad plan arguments");
+  *out = nullptr;
+  int st;
+  pcf_ctx* c = resolve_ctx(ctx, &st);
+  if (!c) return st;
+  pcf_plan* p = new pcf_plan();
+  p->ctx = c;
+  p->n = n;
+  p->npaths.resize(n);
+  p->mu_g.resize(n);
+  p->disc.resize(n);
+  p->use_cv.resize(n);
+  p->out_slot.resize(n);
+  Group g[3];
+  g[0].method = MC_EUR;
+  g[1].method = MC_ASIA;
+  g[2].method = MC_BASKET;
+  for (int i = 0; i < n; ++i) {
+    const int m = reqs[i].method;
+    if (m < 0 || m > 2) {
+      delete p;
+      return set_error(PCF_EINVAL, "request %d: method %d not supported in a batch", i, m);
+    }
+    McContract k;
+    st = build_request(c, reqs[i], i, k, g[m].fb, p->mu_g[i], p->disc[i]);
+    if (st) {
+      delete p;
+      return st;
+    }
+    if (m == PCF_METHOD_BASKET) g[m].max_d = std::max(g[m].max_d, reqs[i].assets);
+    p->npaths[i] = reqs[i].N;
+    p->use_cv[i] = reqs[i].use_cv != 0;
+    g[m].cs.push_back(k);
+    g[m].req.push_back(i);
+  }
+  // Longest items first: the queue then ends on short items (load balance).
+  for (Group& gr : g) {
+    std::vector<int> ord(gr.cs.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int b) { return gr.cs[a].M > gr.cs[b].M; });
+    std::vector<McContract> cs2;
+    std::vector<int> req2;
+    for (int o : ord) {
+      cs2.push_back(gr.cs[o]);
+      req2.push_back(gr.req[o]);
+    }
+    gr.cs.swap(cs2);
+    gr.req.swap(req2);
+    if (!gr.cs.empty()) p->groups.push_back(gr);
+  }
+  // Device layout: per group [contracts | item_start | factors | partials],
+  // then all tickets+queues, then the out table (n x kMoments).
+  size_t off = 0;
+  std::vector<size_t> o_con, o_start, o_fb, o_part, o_tick;
+  size_t ticket_words = 0;
+  for (Group& gr : p->groups) {
+    const int C = (int)gr.cs.size();
+    gr.start.assign((size_t)C + 1, 0);
+    for (int i = 0; i < C; ++i) {
+      if ((long long)gr.start[i] + gr.cs[i].items > 0x7fffffffLL) {
+        delete p;
+        return set_error(PCF_EINVAL, "batch has too many work items");
+      }
+      gr.start[i + 1] = gr.start[i] + gr.cs[i].items;
+    }
+    o_con.push_back(off);
+    off = a256(off + sizeof(McContract) * C);
+    o_start.push_back(off);
+    off = a256(off + sizeof(int) * (C + 1));
+    o_fb.push_back(off);
+    off = a256(off + sizeof(float) * gr.fb.size());
+    o_part.push_back(off);
+    off = a256(off + sizeof(double) * kMoments * (size_t)gr.start[C]);
+    o_tick.push_back(ticket_words);
+    ticket_words += (size_t)C + 1;
+  }
+  const size_t o_tickets = off;
+  p->tickets_bytes = sizeof(unsigned) * ticket_words;
+  off = a256(off + p->tickets_bytes);
+  const size_t o_out = off;
+  off = a256(off + sizeof(double) * kMoments * (size_t)std::max(n, 1));
+  if (c->budget_bytes && off > c->budget_bytes) {
+    delete p;
+    return set_error(PCF_ENOMEM, "plan needs %zu device bytes, over the context budget", off);
+  }
+  st = cuda_status(cudaMalloc(&p->d_mem, off), "cudaMalloc(plan)");
+  if (!st) st = cuda_status(cudaMallocHost((void**)&p->h_out,
+                                           sizeof(double) * kMoments * std::max(n, 1)),
+                            "cudaMallocHost(plan)");
+  if (st) {
+    pcf_plan_destroy(p);
+    return st;
+  }
+  char* d = (char*)p->d_mem;
+  p->d_tickets = (unsigned*)(d + o_tickets);
+  p->d_out = (double*)(d + o_out);
+  // Upload every table with one staging buffer.
+  std::vector<char> host(o_tickets, 0);
+  int row = 0;
+  for (size_t gi = 0; gi < p->groups.size(); ++gi) {
+    Group& gr = p->groups[gi];
+    const int C = (int)gr.cs.size();
+    memcpy(&host[o_con[gi]], gr.cs.data(), sizeof(McContract) * C);
+    memcpy(&host[o_start[gi]], gr.start.data(), sizeof(int) * (C + 1));
+    if (!gr.fb.empty()) memcpy(&host[o_fb[gi]], gr.fb.data(), sizeof(float) * gr.fb.size());
+    for (int i = 0; i < C; ++i) p->out_slot[gr.req[i]] = row + i;
+    McLaunch& L = gr.L;
+    L.contracts = (const McContract*)(d + o_con[gi]);
+    L.item_start = (const int*)(d + o_start[gi]);
+    L.basket_data = (const float*)(d + o_fb[gi]);
+    L.ncontracts = C;
+    L.total_items = gr.start[C];
+    L.partial = (double*)(d + o_part[gi]);
+    L.tickets = p->d_tickets + o_tick[gi];
+    L.queue = L.tickets + C;
+    L.out = p->d_out + (size_t)row * kMoments;
+    L.persistent = 1;
+    gr.grid = std::min(L.total_items, c->sm_count * mc_max_active_blocks(gr.method, gr.max_d));
+    row += C;
+  }
+  if (o_tickets) {
+    st = cuda_status(cudaMemcpyAsync(d, host.data(), o_tickets, cudaMemcpyHostToDevice,
+                                     c->stream),
+                     "H2D plan tables");
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "plan upload");
+    if (st) {
+      pcf_plan_destroy(p);
+      return st;
+    }
+  }
+  *out = p;
+  return PCF_OK;
+}
+
+int pcf_plan_launch(pcf_plan* p) {
+  if (!p) return set_error(PCF_EINVAL, "plan is NULL");
+  pcf_ctx* c = p->ctx;
+  cudaSetDevice(c->device);
+  if (p->tickets_bytes) {
+    int st = cuda_status(cudaMemsetAsync(p->d_tickets, 0, p->tickets_bytes, c->stream),
+                         "memset tickets");
+    if (st) return st;
+  }
+  for (Group& gr : p->groups) {
+    int st = cuda_status(launch_mc(gr.method, gr.L, gr.grid, gr.max_d, c->stream),
+                         "batch kernel launch");
+    if (st) return st;
+    c->launches += 1;
+  }
+  return PCF_OK;
+}
+
+int pcf_plan_kernel_count(const pcf_plan* p) { return p ? (int)p->groups.size() : 0; }
+
+int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
+  if (!p || (p->n && !results)) return set_error(PCF_EINVAL, "bad arguments");
+  pcf_ctx* c = p->ctx;
+  cudaSetDevice(c->device);
+  if (p->n == 0) return PCF_OK;
+  int st = cuda_status(cudaMemcpyAsync(p->h_out, p->d_out, sizeof(double) * kMoments * p->n,
+                                       cudaMemcpyDeviceToHost, c->stream),
+                       "D2H batch results");
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "batch kernels");
+  if (st) return st;
+  for (int i = 0; i < p->n; ++i)
+    fill_result(p->h_out + (size_t)p->out_slot[i] * kMoments, p->npaths[i], p->mu_g[i],
+                p->disc[i], p->use_cv[i] != 0, &results[i]);
+  return PCF_OK;
+}
+
+int pcf_plan_destroy(pcf_plan* p) {
+  if (!p) return PCF_OK;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  if (p->d_mem) cudaFree(p->d_mem);
+  if (p->h_out) cudaFreeHost(p->h_out);
+  delete p;
+  return PCF_OK;
+}
+
+int pcf_price_batch(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_mc_result* results) {
+  pcf_plan* p = nullptr;
+  int st = pcf_plan_create(ctx, n, reqs, &p);
+  if (st) return st;
+  st = pcf_plan_launch(p);
+  if (!st) st = pcf_plan_results(p, results);
+  pcf_plan_destroy(p);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+// Device building blocks shared by every pricing kernel of the engine:
+// the Philox4x32-10 generator, the FP32 Box-Muller mapping, compensated FP32
+// accumulation, FP64 block reductions with a deterministic "last block"
+// finaliser, and a bounded group barrier for persistent kernels.
+//
+// The random stream is part of the engine's contract: a draw is a pure
+// function of (seed, stream, tag, x, y, lane), so any path can be regenerated
+// on the host by an FP64 harness fed the identical uniforms.
+//   key     = (seed & 0xffffffff, seed >> 32)
+//   counter = (x & 0xffffffff, y, stream, (tag << 16) | ((x >> 32) & 0xffff))
+// Philox4x32-10 follows Salmon et al., "Parallel Random Numbers: As Easy as
+// 1, 2, 3" (SC'11). The reference draws with std::mt19937 +
+// std::normal_distribution (src/mc_eur.cpp:17-20); that generator is
+// sequential, so a reproducible counter-based stream replaces it.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pcf {
+
+enum : uint32_t { TAG_EUR = 1, TAG_ASIA = 2, TAG_BASKET = 3, TAG_AMER = 4 };
+
+struct RngKey {
+  uint32_t k0, k1, stream, tag;
+};
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned long long p0 = (unsigned long long)0xD2511F53u * c.x;
+    const unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c.z;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint4 draw_words(const RngKey& k, uint64_t x, uint32_t y) {
+  return philox4x32_10(
+      make_uint4((uint32_t)x, y, k.stream, (k.tag << 16) | ((uint32_t)(x >> 32) & 0xffffu)),
+      k.k0, k.k1);
+}
+
+// u = (2*(w >> 9) + 1) * 2^-24, exactly: 1.m - (1 - 2^-24) is an exact
+// subtraction (Sterbenz), so no integer-to-float conversion is needed.
+__device__ __forceinline__ float uniform_open(uint32_t w) {
+  return __uint_as_float(0x3f800000u | (w >> 9)) - 0.99999994f;
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sin_approx(float x) {
+  float y;
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float cos_approx(float x) {
+  float y;
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Box-Muller on two uniform pairs: (z0,z1) from (w0,w1), (z2,z3) from (w2,w3).
+// z = sqrt(-2 ln u0) * (cos, sin)(pi * (2 u1 - 1)).
+__device__ __forceinline__ float4 normals4(uint4 w) {
+  const float kNeg2Ln2 = -1.38629436112f;  // -2 ln 2: -2 ln u = -2 ln2 * log2 u
+  const float kPi = 3.14159265359f;
+  const float u0 = uniform_open(w.x), u1 = uniform_open(w.y);
+  const float u2 = uniform_open(w.z), u3 = uniform_open(w.w);
+  const float r0 = sqrt_approx(kNeg2Ln2 * lg2_approx(u0));
+  const float r1 = sqrt_approx(kNeg2Ln2 * lg2_approx(u2));
+  const float t0 = kPi * fmaf(2.f, u1, -1.f);
+  const float t1 = kPi * fmaf(2.f, u3, -1.f);
+  return make_float4(r0 * cos_approx(t0), r0 * sin_approx(t0), r1 * cos_approx(t1),
+                     r1 * sin_approx(t1));
+}
+
+__device__ __forceinline__ float lane4(const float4& v, int l) {
+  return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w));
+}
+
+// Kahan-compensated FP32 sum: FP64 is scarce on GB300, so no per-path FP64
+// arithmetic; value() widens once at the end.
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sums K doubles over the block; thread 0 gets the totals in out[]. `sh` must
+// hold 32*K doubles. Deterministic for a fixed block size.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* sh, double (&out)[K]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[wid * K + k] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double x = lane < nw ? sh[lane * K + k] : 0.0;
+      x = warp_sum(x);
+      out[k] = x;
+    }
+  }
+  __syncthreads();
+}
+
+// Deterministic grid reduction by the last block to finish: each block writes
+// its K partials to partial[blockIdx*K..], the block that takes the last
+// ticket sums all partials in block order with one warp and writes out[K],
+// then re-arms the ticket for the next launch. Call with the block's totals
+// in tot[] on thread 0. Returns true in the finalising block.
+template <int K>
+__device__ __forceinline__ void grid_finalize(const double (&tot)[K], double* partial,
+                                              unsigned int* ticket, double* out,
+                                              int nblocks, int block_id) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) partial[(size_t)block_id * K + k] = tot[k];
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    am_last = (t == (unsigned int)nblocks - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double x = 0.0;
+      for (int b = lane; b < nblocks; b += 32) x += ((volatile double*)partial)[(size_t)b * K + k];
+      x = warp_sum(x);
+      if (lane == 0) out[k] = x;
+    }
+    if (lane == 0) *ticket = 0u;
+  }
+}
+
+// Group barrier for a persistent kernel whose blocks are co-resident (the
+// host launches it cooperatively). `counter` only grows, so no reset race:
+// arrival number a (0-based) waits until the count reaches (a/G + 1)*G. The
+// wait is bounded: after `limit` polls it raises *err and returns false.
+__device__ __forceinline__ bool group_barrier(unsigned int* counter, unsigned int G,
+                                              int* err, unsigned int limit) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    __threadfence();
+    const unsigned int a = atomicAdd(counter, 1u);
+    const unsigned int target = (a / G + 1u) * G;
+    unsigned int polls = 0;
+    while (true) {
+      const unsigned int c = *((volatile unsigned int*)counter);
+      if ((int)(c - target) >= 0) break;
+      if (*((volatile int*)err) != 0 || ++polls > limit) {
+        atomicExch(err, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+}  // namespace pcf
