@@ -118,6 +118,40 @@ PCF_API int pcf_mc_basket(pcf_ctx* ctx, int d, const double* S0, const double* s
                   int payoff_fun, int scale_by_sqrt_T, unsigned long long seed, int use_cv,
                   pcf_mc_result* out);
 
+/* American option by Longstaff-Schwartz least squares, M exercise dates,
+ * antithetic path pairs (n, n + N/2); N must be even.
+ * Replaces double mc_amer(S0,E,r,sigma,T,N,M,payoff_fun), src/mc_amer.cpp:5-114
+ * (OpenMP: src/mc_amer_omp.cpp:5-117; paths: include/common.h:168-208).
+ * ref_exercise = 0 exercises at payoff(S) (correct LSM); 1 reproduces the
+ * reference's exercise value payoff(S - E, E) of src/mc_amer.cpp:100, which
+ * makes its puts far too high. price = max(payoff(S0), mean discounted cash
+ * flow) as src/mc_amer.cpp:113. Control variate: the discounted European
+ * payoff at T (mean = Black-Scholes). */
+PCF_API int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+                        long long N, int M, int payoff_fun, int ref_exercise,
+                        unsigned long long seed, int use_cv, pcf_mc_result* out);
+
+/* European option by the closed binomial sum on the reference's
+ * beta-parametrised lattice (u = beta + sqrt(beta^2 - 1), d = 1/u).
+ * Replaces double binom(S0,E,r,sigma,T,N,payoff_fun), src/binom_embar.cpp:5-50
+ * (OpenMP: src/binom_embar_omp.cpp:5-53), with comb() of include/common.h:63-72.
+ * mode 0 reproduces the reference's FP64 result term by term, including the
+ * rounding of its sequential log C(N,i) accumulator (parity 1e-10 relative);
+ * mode 1 computes each binomial weight accurately (Loader's saddle-point
+ * formula) and so differs from the reference by the reference's own
+ * rounding drift. 1 <= N <= 1,000,000. */
+typedef struct pcf_binom_contract {
+  double S0, E, r, sigma, T;
+  int N;
+  int payoff_fun;
+} pcf_binom_contract;
+
+PCF_API int pcf_binom_embar(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+                            int N, int payoff_fun, int mode, double* price);
+/* n contracts of uneven N in one launch; prices[n]. */
+PCF_API int pcf_binom_embar_batch(pcf_ctx* ctx, int n, const pcf_binom_contract* contracts,
+                                  int mode, double* prices);
+
 /* ---- Batched pricing -----------------------------------------------------
  * The reference prices one contract per process run (one main() per price).
  * A batch prices many contracts of mixed methods, uneven path and step

@@ -7,8 +7,12 @@ the reference's.
 from .api import (  # noqa: F401
     Context,
     Plan,
+    binom_embar,
+    binom_embar_batch,
     price_batch,
     request,
+    mc_amer,
+    mc_amer_result,
     mc_asia,
     mc_asia_result,
     mc_basket_result,

@@ -78,6 +78,12 @@ class McRequest(C.Structure):
     ]
 
 
+class BinomContract(C.Structure):
+    _fields_ = [("S0", C.c_double), ("E", C.c_double), ("r", C.c_double),
+                ("sigma", C.c_double), ("T", C.c_double), ("N", C.c_int),
+                ("payoff_fun", C.c_int)]
+
+
 _D = C.c_double
 _LL = C.c_longlong
 _ULL = C.c_ulonglong
@@ -101,6 +107,10 @@ SIGNATURES = {
                               C.POINTER(McResult)]),
     "pcf_mc_basket": (_I, [_P, _I, _PD, _PD, _PD, _D, _D, _D, _LL, _I, _I, _ULL, _I,
                            C.POINTER(McResult)]),
+    "pcf_mc_amer": (_I, [_P, _D, _D, _D, _D, _D, _LL, _I, _I, _I, _ULL, _I,
+                         C.POINTER(McResult)]),
+    "pcf_binom_embar": (_I, [_P, _D, _D, _D, _D, _D, _I, _I, _I, _PD]),
+    "pcf_binom_embar_batch": (_I, [_P, _I, C.POINTER(BinomContract), _I, _PD]),
     "pcf_plan_create": (_I, [_P, _I, C.POINTER(McRequest), C.POINTER(_P)]),
     "pcf_plan_launch": (_I, [_P]),
     "pcf_plan_results": (_I, [_P, C.POINTER(McResult)]),

@@ -8,6 +8,8 @@ does:
     mc_eur_multi(S0, E, r, sigma, T, N, payoff_fun, assets, rho)
                                                           src/mc_eur_multi.cpp:6-35
     mc_asia(S0, E, r, sigma, T, N, M, payoff_fun)        src/mc_asia.cpp:5-40
+    mc_amer(S0, E, r, sigma, T, N, M, payoff_fun)        src/mc_amer.cpp:5-114
+    binom_embar(S0, E, r, sigma, T, N, payoff_fun)       src/binom_embar.cpp:5-50
 
 payoff_fun is +1/-1 (the reference's encoding, include/common.h:56-60) or
 the strings "call"/"put" its command lines accept (src/mc_eur.cpp:39-42).
@@ -120,6 +122,49 @@ def mc_eur_multi(S0, E, r, sigma, T, N, payoff_fun, assets, rho, *, seed=0, use_
                  ctx=None) -> float:
     return mc_eur_multi_result(S0, E, r, sigma, T, N, payoff_fun, assets, rho, seed=seed,
                                use_cv=use_cv, ctx=ctx).price
+
+
+def mc_amer_result(S0, E, r, sigma, T, N, M, payoff_fun, *, ref_exercise=False, seed=0,
+                   use_cv=False, ctx=None):
+    lib = _lib.load()
+    out = _lib.McResult()
+    _lib.check(lib.pcf_mc_amer(_h(ctx), S0, E, r, sigma, T, int(N), int(M),
+                               payoff_code(payoff_fun), int(bool(ref_exercise)), int(seed),
+                               int(bool(use_cv)), C.byref(out)))
+    return out
+
+
+def mc_amer(S0, E, r, sigma, T, N, M, payoff_fun, *, ref_exercise=False, seed=0, use_cv=False,
+            ctx=None) -> float:
+    """src/mc_amer.cpp:5-114. ref_exercise=True reproduces the reference's
+    exercise value payoff(S - E, E) (src/mc_amer.cpp:100)."""
+    return mc_amer_result(S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise=ref_exercise,
+                          seed=seed, use_cv=use_cv, ctx=ctx).price
+
+
+BINOM_MODES = {"reference": 0, "accurate": 1}
+
+
+def binom_embar(S0, E, r, sigma, T, N, payoff_fun, *, mode="reference", ctx=None) -> float:
+    """src/binom_embar.cpp:5-50 (function binom). mode "reference" reproduces
+    the reference's FP64 result; "accurate" uses exact-to-rounding weights."""
+    lib = _lib.load()
+    out = C.c_double()
+    _lib.check(lib.pcf_binom_embar(_h(ctx), S0, E, r, sigma, T, int(N), payoff_code(payoff_fun),
+                                   BINOM_MODES.get(mode, mode), C.byref(out)))
+    return out.value
+
+
+def binom_embar_batch(contracts, *, mode="reference", ctx=None) -> list:
+    """contracts: iterable of (S0, E, r, sigma, T, N, payoff_fun); one launch."""
+    lib = _lib.load()
+    cs = list(contracts)
+    arr = (_lib.BinomContract * len(cs))()
+    for k, (S0, E, r, sigma, T, N, pf) in enumerate(cs):
+        arr[k] = _lib.BinomContract(S0, E, r, sigma, T, int(N), payoff_code(pf))
+    out = (C.c_double * len(cs))()
+    _lib.check(lib.pcf_binom_embar_batch(_h(ctx), len(cs), arr, BINOM_MODES.get(mode, mode), out))
+    return list(out)
 
 
 METHODS = {"eur": _lib.METHOD_EUR, "asia": _lib.METHOD_ASIA, "basket": _lib.METHOD_BASKET,

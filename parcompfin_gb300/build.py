@@ -28,7 +28,7 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler"
 SOURCES = [
     ("mc_kernels.cu", []),
     ("lsm.cu", []),
-    ("binom.cu", ["-fmad=false"]),
+    ("binom.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("pcf_api.cpp", []),
     ("pcf_batch.cpp", []),
     ("pcf_math.cpp", []),

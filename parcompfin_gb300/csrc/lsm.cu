@@ -1,0 +1,537 @@
+// Longstaff-Schwartz American pricing (the reference's mc_amer) on one GPU.
+//
+// Reference: src/mc_amer.cpp:5-114 (serial), src/mc_amer_omp.cpp:5-117, with
+// pathsfinder() of include/common.h:168-208 and the 3x3 solve of
+// include/common.h:98-141. The MPI build reduces the seven regression sums
+// and the in-the-money count to rank 0 and broadcasts three coefficients per
+// date (src/mc_amer_mpi.cpp:82-131). Here the same exchange is a grid-wide
+// FP64 reduction inside one persistent kernel.
+//
+// One cooperative launch per contract, at most one 512-thread block per SM:
+//   forward   each thread generates its antithetic pairs (path p takes +z,
+//             path p + H takes -z, as pathsfinder pairs them) and writes
+//             S(date m), m = 1..M, to an FP32 time-major path matrix in HBM
+//             (row m-1; plus half at columns [0, Hp), minus half at
+//             [Hp, 2Hp), Hp = H rounded up to 4), coalesced across the warp;
+//   backward  for m = M-1..1: the block's slice of row m-1 (two contiguous
+//             runs) arrives in shared memory by TMA bulk copy. The copy for
+//             date m-1 is issued as soon as date m's has landed, so HBM
+//             latency hides behind the date's reduction and barrier. The
+//             block accumulates the 8 regression sums of its in-the-money
+//             paths, publishes one FP64 partial, waits at a bounded group
+//             barrier, reduces all partials in block order (every block gets
+//             the same bits), solves the normal equations by the adjugate
+//             formula and updates the exercise decision of its paths from the
+//             same shared-memory slice;
+//   final     discounted cash flows and the European control variate are
+//             reduced with the deterministic last-block finaliser.
+// Per-path state (cash flow, exercise date) stays in shared memory for the
+// whole sweep. The regression basis is {1, x, x^2} with x = (S - E)/E: the
+// reference's S - E rescaled, the same fitted values in exact arithmetic.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "pcf_api_internal.h"
+#include "pcf_device.cuh"
+#include "pcf_math.h"
+
+namespace pcf {
+
+namespace {
+
+constexpr int kLsmBlock = 512;
+constexpr int kRegSums = 8;  // n, x, x^2, x^3, x^4, y, y x, y x^2
+constexpr size_t kLsmMaxSmem = 227 * 1024;
+
+struct LsmParams {
+  float pf, nK, E, invE;  // payoff = max(pf S + nK, 0); x = (S - E) * invE
+  float a2, b2, l2S0;     // per-date log2 drift / vol, log2 S0
+  float gdisc;            // exp(-rT), for the control variate
+  int M, ref_exercise;
+  long long H;            // antithetic pairs = N / 2
+  long long Hp;           // H rounded up to a multiple of 4
+  int pairs_per_block;    // PB, a multiple of 4
+  int nblocks;
+  uint32_t seed_lo, seed_hi, stream;
+  unsigned wait_limit;       // group-barrier polls before giving up
+  unsigned copy_wait_limit;  // mbarrier polls before giving up on a bulk copy
+  float* paths;           // M rows of 2*Hp floats
+  const float* dtab;      // exp(-r dt k), k = 0..M
+  double* partial;        // 2 x nblocks x kRegSums
+  double* fpartial;       // nblocks x kMoments
+  unsigned* barrier;
+  unsigned* ticket;
+  int* err;               // 1: a barrier wait gave up, 2: a bulk copy wait gave up
+  int* singular;          // dates whose normal equations had det <= 0
+  double* out;            // kMoments sums
+};
+
+__device__ __forceinline__ float lsm_payoff(const LsmParams& P, float S) {
+  return fmaxf(fmaf(P.pf, S, P.nK), 0.f);
+}
+
+// include/common.h:98-141: adjugate over the determinant, then the mat-vec
+// product (one reciprocal instead of nine divisions).
+__device__ bool solve3(const double* a, double* coef) {
+  const double x[3][3] = {{a[0], a[1], a[2]}, {a[1], a[2], a[3]}, {a[2], a[3], a[4]}};
+  const double y[3] = {a[5], a[6], a[7]};
+  double det = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    det += x[0][i] * (x[1][(i + 1) % 3] * x[2][(i + 2) % 3] - x[1][(i + 2) % 3] * x[2][(i + 1) % 3]);
+  if (!(det > 0)) return false;
+  const double rd = 1.0 / det;
+  double inv[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      inv[j][i] = ((x[(j + 1) % 3][(i + 1) % 3] * x[(j + 2) % 3][(i + 2) % 3]) -
+                   (x[(j + 1) % 3][(i + 2) % 3] * x[(j + 2) % 3][(i + 1) % 3])) * rd;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) coef[i] = inv[i][0] * y[0] + inv[i][1] * y[1] + inv[i][2] * y[2];
+  return true;
+}
+
+struct LsmSmem {
+  uint64_t* bar;           // 2 mbarriers
+  float* dt;               // M+1
+  float* cf;               // 2*PB
+  unsigned short* tau;     // 2*PB
+  float* buf[2];           // 2 x 2*PB path slices
+};
+
+__device__ __forceinline__ LsmSmem carve(unsigned char* base, int PB, int M) {
+  LsmSmem s;
+  size_t o = 0;
+  s.bar = (uint64_t*)(base + o);
+  o += 16;
+  s.dt = (float*)(base + o);
+  o += ((size_t)(M + 1) * 4 + 15) & ~(size_t)15;
+  s.cf = (float*)(base + o);
+  o += (size_t)2 * PB * 4;
+  s.tau = (unsigned short*)(base + o);
+  o += ((size_t)2 * PB * 2 + 15) & ~(size_t)15;
+  s.buf[0] = (float*)(base + o);
+  o += (size_t)2 * PB * 4;
+  s.buf[1] = (float*)(base + o);
+  return s;
+}
+
+// Bulk-copies the block's slice of row r (pairs [p0, p0 + nbr)) to dst:
+// plus half to dst[0..nbr), minus half to dst[PB..PB + nbr).
+__device__ __forceinline__ void issue_row(const LsmParams& P, const LsmSmem& S, int r,
+                                          long long p0, int nbr, int PB, float* dst,
+                                          uint64_t* bar) {
+  const float* row = P.paths + (size_t)r * 2 * P.Hp;
+  const uint32_t bytes = (uint32_t)nbr * 4u;
+  mbar_arrive_expect_tx(bar, 2u * bytes);
+  bulk_g2s(dst, row + p0, bytes, bar);
+  bulk_g2s(dst + PB, row + P.Hp + p0, bytes, bar);
+}
+
+// Adds the regression sums of the in-the-money paths of one slice entry.
+__device__ __forceinline__ void reg_accumulate(const LsmParams& P, float Sv, float y, float* acc) {
+  const float x = (Sv - P.E) * P.invE;
+  const float x2 = x * x;
+  acc[0] += 1.f;
+  acc[1] += x;
+  acc[2] += x2;
+  acc[3] = fmaf(x2, x, acc[3]);
+  acc[4] = fmaf(x2, x2, acc[4]);
+  acc[5] += y;
+  acc[6] = fmaf(y, x, acc[6]);
+  acc[7] = fmaf(y, x2, acc[7]);
+}
+
+// Block reduction of the regression sums for date m, publication of the
+// block's partial, the bounded group barrier, the grid reduction (every block
+// sums all partials in block order, so all blocks get the same bits) and the
+// 3x3 solve. Leaves the date's mode and coefficients in shared memory. When
+// `next_row` >= 0, thread 0 issues the bulk copy of that row into `next_buf`
+// once every thread is past the slice that buffer held. Returns false if the
+// barrier wait gave up.
+__device__ bool lsm_regress(const LsmParams& P, const LsmSmem& S, float (&acc)[kRegSums], int m,
+                            int b, DF* sh, double* s_coef, int* s_mode, int next_row, long long p0,
+                            int nbr, int PB, float* next_buf, uint64_t* next_bar) {
+  DF v[kRegSums], tot[kRegSums];
+#pragma unroll
+  for (int q = 0; q < kRegSums; ++q) v[q] = DF{acc[q], 0.f};
+  block_sum_df<kRegSums>(v, sh, tot);  // ends with __syncthreads: slices are free
+  float2* slot = (float2*)P.partial + (size_t)(m & 1) * P.nblocks * kRegSums;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) slot[(size_t)b * kRegSums + q] = make_float2(tot[q].hi, tot[q].lo);
+    if (next_row >= 0 && nbr > 0) issue_row(P, S, next_row, p0, nbr, PB, next_buf, next_bar);
+  }
+  if (!group_barrier(P.barrier, (unsigned)P.nblocks, P.err, P.wait_limit)) return false;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    DF g[kRegSums];
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) g[q] = DF{0.f, 0.f};
+    for (int bb = lane; bb < P.nblocks; bb += 32) {
+      const float4* r4 = (const float4*)(slot + (size_t)bb * kRegSums);
+      float4 a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = __ldcg(r4 + u);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        g[2 * u] = df_add(g[2 * u], DF{a[u].x, a[u].y});
+        g[2 * u + 1] = df_add(g[2 * u + 1], DF{a[u].z, a[u].w});
+      }
+    }
+    double t[kRegSums];
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) t[q] = df_value(warp_sum_df(g[q]));
+    if (lane == 0) {
+      if (t[0] == 0.0) {
+        *s_mode = 0;
+      } else if (t[0] <= 2.0) {
+        *s_mode = 1;
+      } else {
+        double c[3];
+        if (solve3(t, c)) {
+          *s_mode = 2;
+          s_coef[0] = c[0];
+          s_coef[1] = c[1];
+          s_coef[2] = c[2];
+        } else {
+          *s_mode = 0;
+          if (b == 0) atomicAdd(P.singular, 1);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// Exercise decision of one path at date m (src/mc_amer.cpp:73-106).
+__device__ __forceinline__ void lsm_update(const LsmParams& P, const LsmSmem& S, int s, float Sv,
+                                           int m, int mode, float c0, float c1, float c2) {
+  const float pv = lsm_payoff(P, Sv);
+  if (pv > 0.f) {
+    float cont, ex = pv;
+    if (mode == 1) {
+      cont = S.cf[s] * S.dt[S.tau[s] - m];
+    } else {
+      const float x = (Sv - P.E) * P.invE;
+      cont = fmaf(fmaf(c2, x, c1), x, c0);
+      // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E).
+      if (P.ref_exercise) ex = fmaxf(P.pf * (Sv - 2.f * P.E), 0.f);
+    }
+    if (ex > cont) {
+      S.cf[s] = ex;
+      S.tau[s] = (unsigned short)m;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int PB = P.pairs_per_block;
+  const int M = P.M;
+  const LsmSmem S = carve(smem_raw, PB, M);
+  __shared__ DF sh[32 * kRegSums];
+  __shared__ double s_coef[3];
+  __shared__ int s_mode;  // 0 skip date, 1 few ITM paths, 2 regression
+  __shared__ int s_ok;
+
+  const int b = blockIdx.x;
+  const long long p0 = (long long)b * PB;
+  const int nb = (int)max(0LL, min((long long)PB, P.H - p0));  // pairs in this block
+  const int nbr = (nb + 3) & ~3;                                // bulk-copy width
+  for (int k = threadIdx.x; k <= M; k += kLsmBlock) S.dt[k] = P.dtab[k];
+  if (threadIdx.x == 0) {
+    mbar_init(&S.bar[0], 1);
+    mbar_init(&S.bar[1], 1);
+    fence_mbar_init();
+  }
+
+  // ---- forward: generate and store paths ----
+  const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
+  for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+    const long long p = p0 + i;
+    float Lp = 0.f, Lm = 0.f, Sp = 0.f, Sm = 0.f;
+    float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int m = 1; m <= M; ++m) {
+      if (((m - 1) & 3) == 0) z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)((m - 1) >> 2)));
+      const float z = lane4(z4, (m - 1) & 3);
+      Lp += fmaf(P.b2, z, P.a2);
+      Lm += fmaf(-P.b2, z, P.a2);
+      Sp = ex2_approx(P.l2S0 + Lp);
+      Sm = ex2_approx(P.l2S0 + Lm);
+      float* row = P.paths + (size_t)(m - 1) * 2 * P.Hp;
+      row[p] = Sp;
+      row[P.Hp + p] = Sm;
+    }
+    S.cf[i] = lsm_payoff(P, Sp);
+    S.cf[PB + i] = lsm_payoff(P, Sm);
+    S.tau[i] = (unsigned short)M;
+    S.tau[PB + i] = (unsigned short)M;
+  }
+  // The bulk copies below read what this block's threads just stored.
+  fence_proxy_async_global();
+  __syncthreads();
+
+  // Buffer schedule: date d's slice sits in buf[(M - 1 - d) & 1]. Thread 0
+  // owns the copies; pending[k] says a copy into buf[k] is in flight.
+  bool pending[2] = {false, false};
+  uint32_t parity[2] = {0u, 0u};
+  bool alive = true;
+  auto wait_buf = [&](int k) {  // thread 0 only
+    if (!pending[k]) return true;
+    if (!mbar_wait(&S.bar[k], parity[k], P.copy_wait_limit)) return false;
+    parity[k] ^= 1u;
+    pending[k] = false;
+    return true;
+  };
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    if (nbr > 0) {
+      issue_row(P, S, M - 2, p0, nbr, PB, S.buf[0], &S.bar[0]);  // date M-1
+      pending[0] = true;
+      if (!wait_buf(0)) {
+        atomicExch(P.err, 2);
+        s_ok = 0;
+      }
+    }
+  }
+  __syncthreads();
+  alive = s_ok != 0;
+
+  // Sums for date M-1 (the only date without a preceding update pass).
+  if (alive) {
+    float acc[kRegSums];
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
+    const float* sl = S.buf[0];
+    for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int s = h * PB + i;
+        const float Sv = sl[s];
+        if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * S.dt[S.tau[s] - (M - 1)], acc);
+      }
+    }
+    if (threadIdx.x == 0 && M - 2 >= 1 && nbr > 0) pending[1] = true;  // issued in lsm_regress
+    alive = lsm_regress(P, S, acc, M - 1, b, sh, s_coef, &s_mode, M - 2 >= 1 ? M - 3 : -1, p0,
+                        nbr, PB, S.buf[1], &S.bar[1]);
+  }
+
+  // Date m: update with date m's coefficients, fused with the sums of date m-1.
+  for (int m = M - 1; m >= 1 && alive; --m) {
+    const int k = (M - 1 - m) & 1;
+    const bool has_next = m > 1;
+    if (has_next) {
+      if (threadIdx.x == 0) {
+        s_ok = 1;
+        if (nbr > 0 && !wait_buf(k ^ 1)) {
+          atomicExch(P.err, 2);
+          s_ok = 0;
+        }
+      }
+      __syncthreads();
+      if (!s_ok) {
+        alive = false;
+        break;
+      }
+    }
+    const int mode = s_mode;
+    const float c0 = (float)s_coef[0], c1 = (float)s_coef[1], c2 = (float)s_coef[2];
+    const float* cur = S.buf[k];
+    const float* nxt = S.buf[k ^ 1];
+    float acc[kRegSums];
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
+    for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int s = h * PB + i;
+        if (mode != 0) lsm_update(P, S, s, cur[s], m, mode, c0, c1, c2);
+        if (has_next) {
+          const float Sv = nxt[s];
+          if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * S.dt[S.tau[s] - (m - 1)], acc);
+        }
+      }
+    }
+    if (!has_next) break;
+    // buf[k] (date m) is free once lsm_regress's block reduction has synced;
+    // date m-2 goes there.
+    const int next_row = m - 2 >= 1 ? m - 3 : -1;
+    if (threadIdx.x == 0 && next_row >= 0 && nbr > 0) pending[k] = true;
+    alive = lsm_regress(P, S, acc, m - 1, b, sh, s_coef, &s_mode, next_row, p0, nbr, PB,
+                        S.buf[k], &S.bar[k]);
+  }
+  __syncthreads();
+  if (!alive) {
+    // Let any bulk copy this block issued land before the block exits.
+    if (threadIdx.x == 0)
+      for (int k = 0; k < 2; ++k)
+        if (pending[k]) mbar_wait(&S.bar[k], parity[k], P.copy_wait_limit);
+    return;
+  }
+
+  // ---- discounted cash flows and the European control variate ----
+  const float* last = P.paths + (size_t)(M - 1) * 2 * P.Hp;
+  KSum sy, syy, sg, sgg, syg;
+  for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int s = h * PB + i;
+      const float y = S.cf[s] * S.dt[S.tau[s]];
+      const float g = P.gdisc * lsm_payoff(P, last[h * P.Hp + p0 + i]);
+      sy.add(y);
+      syy.add(y * y);
+      sg.add(g);
+      sgg.add(g * g);
+      syg.add(y * g);
+    }
+  }
+  DF v[kMoments] = {df_of(sy), df_of(syy), df_of(sg), df_of(sgg), df_of(syg)};
+  DF tot[kMoments];
+  block_sum_df<kMoments>(v, sh, tot);
+  grid_finalize_df<kMoments>(tot, (float2*)P.fpartial, P.ticket, P.out, P.nblocks, b);
+}
+
+size_t lsm_smem(int PB, int M) {
+  return 16 + ((((size_t)M + 1) * 4 + 15) & ~(size_t)15) + (size_t)2 * PB * 4 +
+         (((size_t)2 * PB * 2 + 15) & ~(size_t)15) + (size_t)2 * 2 * PB * 4;
+}
+
+size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+}  // namespace pcf
+
+using namespace pcf;
+
+extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+                           long long N, int M, int payoff_fun, int ref_exercise,
+                           unsigned long long seed, int use_cv, pcf_mc_result* out) {
+  if (!out) return set_error(PCF_EINVAL, "out is NULL");
+  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+  if (st) return st;
+  if (N % 2 != 0)  // include/common.h:180
+    return set_error(PCF_EINVAL, "N needs to be divisible by 2 for finding paths");
+  if (M < 2 || M > 4096) return set_error(PCF_EINVAL, "M must be in [2, 4096]");
+  if (!(E > 0)) return set_error(PCF_EINVAL, "E must be > 0 for the LSM regression basis");
+  pcf_ctx* c = resolve_ctx(ctx, &st);
+  if (!c) return st;
+  const long long H = N / 2;
+  const long long Hp = (H + 3) & ~3LL;
+
+  // Grid: one block per SM at most (each block reduces every partial, so
+  // fewer, fatter blocks are cheaper), at least one pair per thread, all
+  // blocks co-resident (the cooperative launch checks this too).
+  const long long G0 = std::max(1LL, std::min((H + kLsmBlock - 1) / kLsmBlock,
+                                              (long long)c->sm_count));
+  const int PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
+  const int G = (int)((H + PB - 1) / PB);
+  const size_t smem = lsm_smem(PB, M);
+  if (smem > kLsmMaxSmem)
+    return set_error(PCF_EINVAL, "N = %lld is too large for one device sweep", N);
+  st = cuda_status(cudaFuncSetAttribute(lsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem),
+                   "lsm smem attribute");
+  if (st) return st;
+  int occ = 0;
+  st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_kernel, kLsmBlock, smem),
+                   "occupancy(lsm)");
+  if (st) return st;
+  if ((long long)occ * c->sm_count < G)
+    return set_error(PCF_EINVAL, "LSM grid of %d blocks cannot be co-resident", G);
+
+  // Resident path matrix: M rows x 2*Hp floats.
+  const size_t paths_bytes = sizeof(float) * (size_t)M * 2 * (size_t)Hp;
+  if (paths_bytes > c->paths_cap) {
+    if (c->d_paths) cudaFree(c->d_paths);
+    c->d_paths = nullptr;
+    c->paths_cap = 0;
+    if (c->budget_bytes && paths_bytes > c->budget_bytes)
+      return set_error(PCF_ENOMEM, "path matrix of %zu bytes exceeds the context budget",
+                       paths_bytes);
+    st = cuda_status(cudaMalloc(&c->d_paths, paths_bytes), "cudaMalloc(path matrix)");
+    if (st) return st;
+    c->paths_cap = paths_bytes;
+  }
+  // Scratch: dtab | partial | fpartial | counters | out.
+  const size_t o_dt = 0;
+  const size_t o_part = a256(o_dt + sizeof(float) * (M + 1));
+  const size_t o_fpart = a256(o_part + sizeof(double) * 2 * G * kRegSums);
+  const size_t o_cnt = a256(o_fpart + sizeof(double) * G * kMoments);
+  const size_t o_out = a256(o_cnt + sizeof(unsigned) * 4);
+  const size_t total = a256(o_out + sizeof(double) * kMoments);
+  st = ctx_ensure(c, total, total);
+  if (st) return st;
+  char* d = (char*)c->d_buf;
+  char* h = (char*)c->h_buf;
+  const double dtd = T / M;
+  for (int k = 0; k <= M; ++k) ((float*)(h + o_dt))[k] = (float)exp(-r * dtd * k);
+  st = cuda_status(cudaMemcpyAsync(d + o_dt, h + o_dt, sizeof(float) * (M + 1),
+                                   cudaMemcpyHostToDevice, c->stream), "H2D dtab");
+  if (!st) st = cuda_status(cudaMemsetAsync(d + o_cnt, 0, sizeof(unsigned) * 4, c->stream),
+                            "memset counters");
+  if (st) return st;
+
+  const double log2e = 1.4426950408889634;
+  LsmParams P;
+  memset(&P, 0, sizeof P);
+  P.pf = (float)payoff_fun;
+  P.nK = (float)(-payoff_fun * E);
+  P.E = (float)E;
+  P.invE = (float)(1.0 / E);
+  P.a2 = (float)((r - 0.5 * sigma * sigma) * dtd * log2e);
+  P.b2 = (float)(sigma * sqrt(dtd) * log2e);
+  P.l2S0 = (float)(log(S0) * log2e);
+  P.gdisc = (float)exp(-r * T);
+  P.M = M;
+  P.ref_exercise = ref_exercise ? 1 : 0;
+  P.H = H;
+  P.Hp = Hp;
+  P.pairs_per_block = PB;
+  P.nblocks = G;
+  P.seed_lo = (uint32_t)seed;
+  P.seed_hi = (uint32_t)(seed >> 32);
+  P.stream = 0;
+  P.wait_limit = 1u << 22;       // ~64 ns sleep + an L2 round trip per poll: seconds
+  P.copy_wait_limit = 1u << 20;  // try_wait polls: far beyond a microsecond-scale copy
+  P.paths = (float*)c->d_paths;
+  P.dtab = (const float*)(d + o_dt);
+  P.partial = (double*)(d + o_part);
+  P.fpartial = (double*)(d + o_fpart);
+  unsigned* cnt = (unsigned*)(d + o_cnt);
+  P.barrier = cnt;
+  P.ticket = cnt + 1;
+  P.err = (int*)(cnt + 2);
+  P.singular = (int*)(cnt + 3);
+  P.out = (double*)(d + o_out);
+  void* args[] = {&P};
+  st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_kernel, dim3(G), dim3(kLsmBlock), args,
+                                               smem, c->stream),
+                   "lsm kernel launch");
+  if (st) return st;
+  c->launches += 1;
+  st = cuda_status(cudaMemcpyAsync(h + o_cnt, d + o_cnt, o_out - o_cnt + sizeof(double) * kMoments,
+                                   cudaMemcpyDeviceToHost, c->stream),
+                   "D2H lsm");
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "lsm kernel");
+  if (st) return st;
+  const int* flags = (const int*)(h + o_cnt);
+  if (flags[2]) return set_error(PCF_ETIMEOUT, "LSM device wait gave up (code %d)", flags[2]);
+  if (flags[3])
+    return set_error(PCF_ESINGULAR, "Detereminant is not > 0 at %d exercise date(s)", flags[3]);
+  const double* s = (const double*)(h + o_out);
+  fill_result(s, N, bs_price(S0, E, r, sigma, T, payoff_fun), 1.0, use_cv != 0, out);
+  // src/mc_amer.cpp:113: the price is at least the immediate exercise value.
+  const double intrinsic = std::max(payoff_fun * (S0 - E), 0.0);
+  out->price = std::max(out->price, intrinsic);
+  out->price_plain = std::max(out->price_plain, intrinsic);
+  if (use_cv) out->price_cv = std::max(out->price_cv, intrinsic);
+  return PCF_OK;
+}

@@ -7,9 +7,14 @@
 // persistently, pulls items from a device queue until it is empty. Per-path
 // arithmetic is FP32: Philox4x32-10 -> Box-Muller -> GBM in the log2 domain
 // (one FMA + one ex2 per step) -> payoff. Each thread accumulates Kahan-
-// compensated FP32 moment sums. Blocks reduce them in FP64 and write one
-// partial per item. The last item of a contract to finish sums that
-// contract's partials in item order, so results do not depend on scheduling.
+// compensated FP32 moment sums. Blocks reduce them as double-floats (FP32
+// hi/lo pairs; the FP64 pipe is slow on GB300) and write one partial per
+// item. The last item of a contract to finish sums that contract's partials
+// in item order and widens to FP64, so results do not depend on scheduling.
+//
+// The kernels are issue-bound (Philox + Box-Muller + GBM is ~50 FP32/INT
+// instructions against 3 SFU operations per path), so the control-variate
+// sums are compiled in only when a launch asks for them (CV template flag).
 //
 // Reference loops these kernels replace:
 //   European  src/mc_eur.cpp:22-26,  src/mc_eur_omp.cpp:24-27
@@ -22,68 +27,82 @@ namespace pcf {
 
 namespace {
 
-__device__ __forceinline__ float payoff(float S, float K, float pf) {
-  return fmaxf(pf * (S - K), 0.f);
-}
-
+// Per-thread moment accumulators. Values are first summed in plain FP32 over
+// a short chunk (a few paths), then each chunk sum is added with Kahan
+// compensation, so the thread total is accurate to a few FP32 ulps.
+template <bool CV>
 struct Moments {
   KSum y, yy, g, gg, yg;
+  __device__ __forceinline__ void flush(float cy, float cyy, float cg, float cgg, float cyg) {
+    y.add(cy);
+    yy.add(cyy);
+    if (CV) {
+      g.add(cg);
+      gg.add(cgg);
+      yg.add(cyg);
+    }
+  }
   __device__ __forceinline__ void add(float Y, float G) {
-    y.add(Y);
-    yy.add(Y * Y);
-    g.add(G);
-    gg.add(G * G);
-    yg.add(Y * G);
+    flush(Y, Y * Y, G, G * G, Y * G);
   }
 };
 
+__device__ __forceinline__ float payoff(const McContract& C, float S) {
+  return fmaxf(fmaf(C.pf, S, C.nK), 0.f);  // max(pf (S - K), 0)
+}
+
 // European: item j covers path quads [j*U, (j+1)*U), U = units_per_item.
 // Quad q's four paths take the four normals of Philox block (x=q, y=0).
-// y = payoff(S_T), g = S_T.
-__device__ __forceinline__ void eur_item(const McContract& C, int j, Moments& mo) {
+// S_T = 2^(log2 S0 + a2 + b2 z); y = payoff(S_T), g = S_T.
+template <bool CV>
+__device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>& mo) {
   const long long nq = (C.N + 3) >> 2;
-  const long long q0 = (long long)j * C.units_per_item;
+  const long long nfull = C.N >> 2;  // quads whose four paths are all < N
+  const long long q0 = (long long)j * C.units_per_item + threadIdx.x;
   const int qpt = C.units_per_item / kBlock;
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_EUR};
-  for (int k = 0; k < qpt; ++k) {
-    const long long q = q0 + threadIdx.x + (long long)k * kBlock;
-    if (q >= nq) break;
-    const float4 z = normals4(draw_words(key, (uint64_t)q, 0u));
-    const long long left = C.N - 4 * q;
-    float s[4];
-    s[0] = C.S0 * ex2_approx(fmaf(C.b2, z.x, C.a2));
-    s[1] = C.S0 * ex2_approx(fmaf(C.b2, z.y, C.a2));
-    s[2] = C.S0 * ex2_approx(fmaf(C.b2, z.z, C.a2));
-    s[3] = C.S0 * ex2_approx(fmaf(C.b2, z.w, C.a2));
-    float ys = 0.f, yys = 0.f, gs = 0.f, ggs = 0.f, ygs = 0.f;
+  const float a2 = C.a2 + C.l2S0;
+  for (int k0 = 0; k0 < qpt; k0 += 4) {
+    float cy = 0.f, cyy = 0.f, cg = 0.f, cgg = 0.f, cyg = 0.f;
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
-      const bool ok = l < left;
-      const float Y = ok ? payoff(s[l], C.K, C.pf) : 0.f;
-      const float G = ok ? s[l] : 0.f;
-      ys += Y;
-      yys = fmaf(Y, Y, yys);
-      gs += G;
-      ggs = fmaf(G, G, ggs);
-      ygs = fmaf(Y, G, ygs);
+    for (int kk = 0; kk < 4; ++kk) {
+      const long long q = q0 + (long long)(k0 + kk) * kBlock;
+      if (k0 + kk < qpt && q < nq) {
+        const float4 z = normals4(draw_words(key, (uint64_t)q, 0u));
+        float s[4] = {ex2_approx(fmaf(C.b2, z.x, a2)), ex2_approx(fmaf(C.b2, z.y, a2)),
+                      ex2_approx(fmaf(C.b2, z.z, a2)), ex2_approx(fmaf(C.b2, z.w, a2))};
+        float y[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) y[l] = payoff(C, s[l]);
+        if (q >= nfull) {  // the one partial quad at the end of the contract
+          const long long left = C.N - 4 * q;
+#pragma unroll
+          for (int l = 0; l < 4; ++l)
+            if (l >= left) y[l] = s[l] = 0.f;
+        }
+        cy += (y[0] + y[1]) + (y[2] + y[3]);
+        cyy = fmaf(y[0], y[0], fmaf(y[1], y[1], fmaf(y[2], y[2], fmaf(y[3], y[3], cyy))));
+        if (CV) {
+          cg += (s[0] + s[1]) + (s[2] + s[3]);
+          cgg = fmaf(s[0], s[0], fmaf(s[1], s[1], fmaf(s[2], s[2], fmaf(s[3], s[3], cgg))));
+          cyg = fmaf(y[0], s[0], fmaf(y[1], s[1], fmaf(y[2], s[2], fmaf(y[3], s[3], cyg))));
+        }
+      }
     }
-    mo.y.add(ys);
-    mo.yy.add(yys);
-    mo.g.add(gs);
-    mo.gg.add(ggs);
-    mo.yg.add(ygs);
+    mo.flush(cy, cyy, cg, cgg, cyg);
   }
 }
 
 // Asian: one path per thread; increment m uses lane m%4 of Philox block
-// (x=path, y=m/4). log2 S is accumulated, S = S0 * 2^L.
+// (x=path, y=m/4). log2(S/S0) is accumulated, S = S0 * 2^L.
 // mode 0 (reference, src/mc_asia.cpp:31-35): I += S_m (c1 + c2 z_m) with S_m
 //   the level before the step; A = I/M.
 // mode 1: I += S_{m+1}; A = I/M (discrete mean of S_1..S_M).
 // g = payoff of the geometric mean exp(sum_m w_m log S_m): mode 0 uses the
 // trapezoid weights (w_M = 1/(2M), S_0's weight multiplies log S0/S0 = 0),
 // mode 1 equal weights 1/M on S_1..S_M.
-__device__ __forceinline__ void asia_item(const McContract& C, int j, Moments& mo) {
+template <bool CV>
+__device__ __forceinline__ void asia_item(const McContract& C, int j, Moments<CV>& mo) {
   const long long n = (long long)j * C.units_per_item + threadIdx.x;
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_ASIA};
   const int M = C.M;
@@ -100,29 +119,29 @@ __device__ __forceinline__ void asia_item(const McContract& C, int j, Moments& m
           const float S = C.S0 * ex2_approx(L);
           I = fmaf(S, fmaf(C.c2, zl, C.c1), I);
           L += fmaf(C.b2, zl, C.a2);
-          lg = fmaf(m == M - 1 ? C.w_last : w, L, lg);
+          if (CV) lg = fmaf(m == M - 1 ? C.w_last : w, L, lg);
         } else {
           L += fmaf(C.b2, zl, C.a2);
           I += C.S0 * ex2_approx(L);
-          lg = fmaf(w, L, lg);
+          if (CV) lg = fmaf(w, L, lg);
         }
       }
     }
   }
   const bool ok = n < C.N;
-  const float Y = ok ? payoff(I * w, C.K, C.pf) : 0.f;
-  const float G = ok ? payoff(C.S0 * ex2_approx(lg), C.K, C.pf) : 0.f;
+  const float Y = ok ? payoff(C, I * w) : 0.f;
+  const float G = (CV && ok) ? payoff(C, C.S0 * ex2_approx(lg)) : 0.f;
   mo.add(Y, G);
 }
 
 // Basket of d <= DMAX assets: one path per thread. Asset a's normal is lane
-// a%4 of Philox block (x=path, y=a/4). x = Lz with the lower Cholesky factor
+// a%4 of Philox block (x=path, y=a/4). x = Lz with the correlation factor
 // staged in shared memory; log2 S_a = l0_a + v_a x_a; y = payoff(mean_a S_a),
 // g = payoff(2^(mean_a log2 S_a)). mode 0: the factor is lower triangular
 // (Cholesky); mode 1: a full factor (eigen-decomposition fallback).
-template <int DMAX>
+template <int DMAX, bool CV>
 __device__ __forceinline__ void basket_item(const McContract& C, int j, const float* fb,
-                                            Moments& mo) {
+                                            Moments<CV>& mo) {
   const long long n = (long long)j * C.units_per_item + threadIdx.x;
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_BASKET};
   const int d = C.M;
@@ -170,8 +189,8 @@ __device__ __forceinline__ void basket_item(const McContract& C, int j, const fl
   }
   const float inv_d = 1.f / (float)d;
   const bool ok = n < C.N;
-  const float Y = ok ? payoff(bsk * inv_d, C.K, C.pf) : 0.f;
-  const float G = ok ? payoff(ex2_approx(geo * inv_d), C.K, C.pf) : 0.f;
+  const float Y = ok ? payoff(C, bsk * inv_d) : 0.f;
+  const float G = (CV && ok) ? payoff(C, ex2_approx(geo * inv_d)) : 0.f;
   mo.add(Y, G);
 }
 
@@ -185,9 +204,9 @@ __device__ __forceinline__ int find_contract(const int* start, int n, int item) 
   return lo;
 }
 
-template <int METHOD, int DMAX>
+template <int METHOD, int DMAX, bool CV>
 __global__ void __launch_bounds__(kBlock) mc_kernel(McLaunch L) {
-  __shared__ double sh[32 * kMoments];
+  __shared__ DF sh[32 * kMoments];
   __shared__ int s_item;
   extern __shared__ float s_fb[];
   for (int iter = 0;; ++iter) {
@@ -205,48 +224,50 @@ __global__ void __launch_bounds__(kBlock) mc_kernel(McLaunch L) {
     const int c = find_contract(L.item_start, L.ncontracts, item);
     const McContract C = L.contracts[c];
     const int j = item - __ldg(L.item_start + c);
-    Moments mo;
+    Moments<CV> mo;
     if (METHOD == MC_EUR) {
-      eur_item(C, j, mo);
+      eur_item<CV>(C, j, mo);
     } else if (METHOD == MC_ASIA) {
-      asia_item(C, j, mo);
+      asia_item<CV>(C, j, mo);
     } else {
       const int d = C.M;
       const float* src = L.basket_data + C.basket_off;
       for (int i = threadIdx.x; i < 2 * d + d * d; i += kBlock) s_fb[i] = src[i];
       __syncthreads();
-      basket_item<DMAX>(C, j, s_fb, mo);
+      basket_item<DMAX, CV>(C, j, s_fb, mo);
       __syncthreads();
     }
-    double v[kMoments] = {mo.y.value(), mo.yy.value(), mo.g.value(), mo.gg.value(),
-                          mo.yg.value()};
-    double tot[kMoments];
-    block_sum<kMoments>(v, sh, tot);
+    DF v[kMoments] = {df_of(mo.y), df_of(mo.yy), df_of(mo.g), df_of(mo.gg), df_of(mo.yg)};
+    DF tot[kMoments];
+    block_sum_df<kMoments>(v, sh, tot);
     const int base = __ldg(L.item_start + c);
-    grid_finalize<kMoments>(tot, L.partial + (size_t)base * kMoments, L.tickets + c,
-                            L.out + (size_t)c * kMoments, C.items, j);
+    grid_finalize_df<kMoments>(tot, (float2*)L.partial + (size_t)base * kMoments, L.tickets + c,
+                               L.out + (size_t)c * kMoments, C.items, j);
     __syncthreads();
   }
 }
 
-template <int METHOD, int DMAX>
+constexpr size_t basket_smem(int dmax) { return (size_t)(2 * dmax + dmax * dmax) * sizeof(float); }
+
+template <int METHOD, int DMAX, bool CV>
 cudaError_t launch_one(const McLaunch& L, int grid, cudaStream_t s) {
-  size_t smem = METHOD == MC_BASKET ? (size_t)(2 * DMAX + DMAX * DMAX) * sizeof(float) : 0;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(mc_kernel<METHOD, DMAX>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  mc_kernel<METHOD, DMAX><<<grid, kBlock, smem, s>>>(L);
+  const size_t smem = METHOD == MC_BASKET ? basket_smem(DMAX) : 0;
+  mc_kernel<METHOD, DMAX, CV><<<grid, kBlock, smem, s>>>(L);
   return cudaGetLastError();
+}
+
+template <int METHOD, int DMAX>
+cudaError_t launch_cv(const McLaunch& L, int grid, cudaStream_t s) {
+  return L.cv ? launch_one<METHOD, DMAX, true>(L, grid, s)
+              : launch_one<METHOD, DMAX, false>(L, grid, s);
 }
 
 template <int METHOD, int DMAX>
 int max_active(void) {
   int n = 0;
-  size_t smem = METHOD == MC_BASKET ? (size_t)(2 * DMAX + DMAX * DMAX) * sizeof(float) : 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mc_kernel<METHOD, DMAX>, kBlock, smem) !=
-      cudaSuccess)
+  const size_t smem = METHOD == MC_BASKET ? basket_smem(DMAX) : 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mc_kernel<METHOD, DMAX, true>, kBlock,
+                                                    smem) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
@@ -256,14 +277,14 @@ int max_active(void) {
 cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, cudaStream_t s) {
   if (grid <= 0) return cudaSuccess;
   switch (m) {
-    case MC_EUR: return launch_one<MC_EUR, 4>(L, grid, s);
-    case MC_ASIA: return launch_one<MC_ASIA, 4>(L, grid, s);
+    case MC_EUR: return launch_cv<MC_EUR, 4>(L, grid, s);
+    case MC_ASIA: return launch_cv<MC_ASIA, 4>(L, grid, s);
     case MC_BASKET:
-      if (max_d <= 4) return launch_one<MC_BASKET, 4>(L, grid, s);
-      if (max_d <= 8) return launch_one<MC_BASKET, 8>(L, grid, s);
-      if (max_d <= 16) return launch_one<MC_BASKET, 16>(L, grid, s);
-      if (max_d <= 32) return launch_one<MC_BASKET, 32>(L, grid, s);
-      if (max_d <= 64) return launch_one<MC_BASKET, 64>(L, grid, s);
+      if (max_d <= 4) return launch_cv<MC_BASKET, 4>(L, grid, s);
+      if (max_d <= 8) return launch_cv<MC_BASKET, 8>(L, grid, s);
+      if (max_d <= 16) return launch_cv<MC_BASKET, 16>(L, grid, s);
+      if (max_d <= 32) return launch_cv<MC_BASKET, 32>(L, grid, s);
+      if (max_d <= 64) return launch_cv<MC_BASKET, 64>(L, grid, s);
       return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;

@@ -90,7 +90,7 @@ pcf_ctx* resolve_ctx(pcf_ctx* ctx, int* status) {
 // Runs one batch of MC contracts of one method and returns the moment sums
 // (C * kMoments doubles). Contracts must have units_per_item and items set.
 int run_mc(pcf_ctx* c, McMethod m, std::vector<McContract>& cs, const std::vector<float>& fb,
-           int max_d, bool persistent, std::vector<double>& sums) {
+           int max_d, bool persistent, bool cv, std::vector<double>& sums) {
   const int C = (int)cs.size();
   std::vector<int> start((size_t)C + 1, 0);
   for (int i = 0; i < C; ++i) {
@@ -133,6 +133,7 @@ int run_mc(pcf_ctx* c, McMethod m, std::vector<McContract>& cs, const std::vecto
   L.queue = L.tickets + C;
   L.out = (double*)(d + o_out);
   L.persistent = persistent ? 1 : 0;
+  L.cv = cv ? 1 : 0;
   int grid = items;
   if (persistent) grid = std::min(items, c->sm_count * mc_max_active_blocks(m, max_d));
   st = cuda_status(launch_mc(m, L, grid, max_d, c->stream), "mc kernel launch");
@@ -189,8 +190,9 @@ static void split_seed(unsigned long long seed, McContract& k) {
 
 int eur_quads_per_thread(const pcf_ctx* c, long long N) {
   const long long nq = (N + 3) / 4;
-  const long long per = nq / ((long long)kBlock * c->sm_count * 8);
-  return (int)std::max(1LL, std::min(64LL, per));
+  long long per = nq / ((long long)kBlock * c->sm_count * 8);
+  per = std::max(1LL, std::min(64LL, per));
+  return (int)(per >= 4 ? per & ~3LL : per);  // chunks of 4 quads per Kahan flush
 }
 
 McContract make_eur(const pcf_ctx* c, double S0, double E, double r, double sigma, double T,
@@ -203,6 +205,8 @@ McContract make_eur(const pcf_ctx* c, double S0, double E, double r, double sigm
   k.pf = (float)pf;
   k.a2 = (float)((r - 0.5 * sigma * sigma) * T * log2e);
   k.b2 = (float)(sigma * sqrt(T) * log2e);
+  k.l2S0 = (float)(log(S0) * log2e);
+  k.nK = (float)(-pf * E);
   k.N = N;
   k.units_per_item = kBlock * eur_quads_per_thread(c, N);
   k.items = (int)(((N + 3) / 4 + k.units_per_item - 1) / k.units_per_item);
@@ -225,6 +229,7 @@ McContract make_asia(double S0, double E, double r, double sigma, double T, long
   k.c1 = (float)(1 + r * dt / 2);
   k.c2 = (float)(sigma * sqrt(dt) / 2);
   k.w_last = (float)(mode == 0 ? 0.5 / M : 1.0 / M);
+  k.nK = (float)(-pf * E);
   k.M = M;
   k.mode = mode;
   k.N = N;
@@ -264,6 +269,7 @@ int make_basket(int d, const double* S0, const double* sig, const double* corr, 
   k.pf = (float)pf;
   k.M = d;
   k.mode = tri ? 0 : 1;
+  k.nK = (float)(-pf * E);
   k.N = N;
   k.units_per_item = kBlock;
   k.items = (int)((N + kBlock - 1) / kBlock);
@@ -359,7 +365,7 @@ int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double
   if (!c) return st;
   std::vector<McContract> cs{make_eur(c, S0, E, r, sigma, T, N, payoff_fun, seed, 0)};
   std::vector<double> sums;
-  st = run_mc(c, MC_EUR, cs, {}, 0, false, sums);
+  st = run_mc(c, MC_EUR, cs, {}, 0, false, use_cv != 0, sums);
   if (st) return st;
   fill_result(sums.data(), N, S0 * exp(r * T), exp(-r * T), use_cv != 0, out);
   return PCF_OK;
@@ -378,7 +384,7 @@ int pcf_mc_asia(pcf_ctx* ctx, double S0, double E, double r, double sigma, doubl
   if (!c) return st;
   std::vector<McContract> cs{make_asia(S0, E, r, sigma, T, N, M, payoff_fun, mode, seed, 0)};
   std::vector<double> sums;
-  st = run_mc(c, MC_ASIA, cs, {}, 0, false, sums);
+  st = run_mc(c, MC_ASIA, cs, {}, 0, false, use_cv != 0, sums);
   if (st) return st;
   fill_result(sums.data(), N, asia_cv_mean(S0, E, r, sigma, T, M, payoff_fun, mode),
               exp(-r * T), use_cv != 0, out);
@@ -402,7 +408,7 @@ int pcf_mc_basket(pcf_ctx* ctx, int d, const double* S0, const double* sigma, co
   if (st) return st;
   std::vector<McContract> cs{k};
   std::vector<double> sums;
-  st = run_mc(c, MC_BASKET, cs, fb, d, false, sums);
+  st = run_mc(c, MC_BASKET, cs, fb, d, false, use_cv != 0, sums);
   if (st) return st;
   fill_result(sums.data(), N, mu_g, exp(-r * T), use_cv != 0, out);
   return PCF_OK;

@@ -24,8 +24,9 @@ struct pcf_ctx {
   void* d_paths = nullptr;
   size_t paths_cap = 0;
   // log((double)n) table for the reference-order binomial sum.
-  double* d_logtab = nullptr;
+  double* d_logtab = nullptr;  // one allocation: log table, prefix tables, ties
   int logtab_n = 0;
+  size_t binom_off[4] = {0, 0, 0, 0};  // offsets of prefix sums, tie offsets, ties, stirlerr
   // Upper bound on device bytes this context may hold (0 = unlimited).
   size_t budget_bytes = 0;
   long long launches = 0;

@@ -217,6 +217,8 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
     L.queue = L.tickets + C;
     L.out = p->d_out + (size_t)row * kMoments;
     L.persistent = 1;
+    L.cv = 0;
+    for (int i = 0; i < C; ++i) L.cv |= p->use_cv[gr.req[i]];
     gr.grid = std::min(L.total_items, c->sm_count * mc_max_active_blocks(gr.method, gr.max_d));
     row += C;
   }

@@ -108,6 +108,101 @@ struct KSum {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// Double-float value hi + lo (two FP32s, ~48 significant bits). GB300's FP64
+// pipe runs at a small fraction of its FP32 rate, so reductions combine
+// partial sums with the error-free TwoSum transformation in FP32 and widen
+// to FP64 only once at the end.
+struct DF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);  // TwoSum error of a.hi + b.hi
+  e += a.lo + b.lo;
+  const float hi = s + e;
+  return DF{hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ DF df_of(const KSum& k) {  // k.s - k.c, exactly
+  const float s = k.s, m = -k.c;
+  const float hi = s + m;
+  const float bb = hi - s;
+  return DF{hi, (s - (hi - bb)) + (m - bb)};
+}
+
+__device__ __forceinline__ double df_value(DF a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ DF warp_sum_df(DF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DF w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = df_add(v, w);
+  }
+  return v;
+}
+
+// Sums K double-floats over the block; thread 0 gets the totals. `sh` must
+// hold 32*K DFs. Deterministic for a fixed block size.
+template <int K>
+__device__ __forceinline__ void block_sum_df(DF (&v)[K], DF* sh, DF (&out)[K]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = warp_sum_df(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[wid * K + k] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      DF x = lane < nw ? sh[lane * K + k] : DF{0.f, 0.f};
+      out[k] = warp_sum_df(x);
+    }
+  }
+  __syncthreads();
+}
+
+// Deterministic last-block finaliser over double-float partials: each block
+// stores its K totals as (hi, lo) pairs in partial[block_id*K..]; the block
+// that takes the last ticket sums all partials in block order with one warp,
+// writes out[k] in FP64 and re-arms the ticket.
+template <int K>
+__device__ __forceinline__ void grid_finalize_df(const DF (&tot)[K], float2* partial,
+                                                 unsigned int* ticket, double* out,
+                                                 int nblocks, int block_id) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      partial[(size_t)block_id * K + k] = make_float2(tot[k].hi, tot[k].lo);
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    am_last = (t == (unsigned int)nblocks - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      DF x{0.f, 0.f};
+      for (int b = lane; b < nblocks; b += 32) {
+        const float2 p = __ldcg(partial + (size_t)b * K + k);
+        x = df_add(x, DF{p.x, p.y});
+      }
+      x = warp_sum_df(x);
+      if (lane == 0) out[k] = df_value(x);
+    }
+    if (lane == 0) *ticket = 0u;
+  }
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -168,6 +263,54 @@ __device__ __forceinline__ void grid_finalize(const double (&tot)[K], double* pa
     }
     if (lane == 0) *ticket = 0u;
   }
+}
+
+// ---- TMA bulk copies (cp.async.bulk) completed on an mbarrier ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+// Makes mbarrier initialisation visible to the async (TMA) proxy.
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this thread's earlier generic-proxy global writes before later
+// async-proxy (TMA) reads of the same memory.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Global -> shared bulk copy; src, dst 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Waits for the mbarrier phase with the given parity; gives up after
+// `limit` polls and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 
 // Group barrier for a persistent kernel whose blocks are co-resident (the

@@ -28,7 +28,9 @@ struct McContract {
   long long N;           // paths
   uint32_t seed_lo, seed_hi, stream, pad;
   int basket_off;        // basket: offset of this contract's factor block
-  int pad2;
+  float nK;              // -pf * K: payoff = max(pf * S + nK, 0)
+  float l2S0;            // log2(S0)
+  float pad2;
 };
 
 // Basket factor block (device): per asset log2(S0_a) + (r - s_a^2/2) T log2e,
@@ -40,10 +42,11 @@ struct McLaunch {
   int ncontracts;
   int total_items;
   unsigned int* queue;     // persistent mode: next item (reset to 0 by the host)
-  double* partial;         // total_items * kMoments
+  double* partial;         // total_items * kMoments slots of 8 bytes (double-float pairs)
   unsigned int* tickets;   // per contract, re-armed by the finaliser
   double* out;             // ncontracts * kMoments
   int persistent;
+  int cv;                  // accumulate the control-variate sums (else they are 0)
 };
 
 enum McMethod { MC_EUR = 0, MC_ASIA = 1, MC_BASKET = 2 };

@@ -36,7 +36,7 @@ def _eur_twin(orc, S0, E, r, sigma, T, N, pf, seed):
 @pytest.mark.parametrize("pf", [1, -1])
 def test_eur_matches_fp64_twin(orc, ctx, N, pf):
     from parcompfin_gb300 import mc_eur_result
-    res = mc_eur_result(100, 100, .05, .2, 1, N, pf, seed=42, ctx=ctx)
+    res = mc_eur_result(100, 100, .05, .2, 1, N, pf, seed=42, use_cv=True, ctx=ctx)
     s = _eur_twin(orc, 100, 100, .05, .2, 1, N, pf, 42)
     assert res.n_paths == N
     for k in range(5):
@@ -45,6 +45,18 @@ def test_eur_matches_fp64_twin(orc, ctx, N, pf):
         else:
             assert rel(res.sums[k], s[k]) < DET_REL, (k, res.sums[k], s[k])
     assert rel(res.price_plain, math.exp(-.05) * s[0] / N) < DET_REL or s[0] == 0
+
+
+def test_plain_and_cv_launches_share_the_payoff_sums(ctx):
+    """The control-variate sums are compiled in only on request; the payoff
+    sums are accumulated the same way either way."""
+    from parcompfin_gb300 import mc_asia_result, mc_eur_result
+    a = mc_eur_result(100, 95, .05, .2, 1, 123_457, 1, seed=3, ctx=ctx)
+    b = mc_eur_result(100, 95, .05, .2, 1, 123_457, 1, seed=3, use_cv=True, ctx=ctx)
+    assert list(a.sums[:2]) == list(b.sums[:2]) and list(a.sums[2:]) == [0.0, 0.0, 0.0]
+    a = mc_asia_result(100, 95, .05, .2, 1, 5000, 12, -1, seed=3, ctx=ctx)
+    b = mc_asia_result(100, 95, .05, .2, 1, 5000, 12, -1, seed=3, use_cv=True, ctx=ctx)
+    assert list(a.sums[:2]) == list(b.sums[:2])
 
 
 def test_eur_config0_against_black_scholes(ctx):
@@ -101,7 +113,8 @@ def _asia_twin(orc, S0, E, r, sig, T, N, M, pf, mode, seed):
 def test_asia_matches_fp64_twin(orc, ctx, mode, N, M):
     from parcompfin_gb300 import mc_asia_result
     for pf in (1, -1):
-        res = mc_asia_result(100, 100, .04, .3, 1.0, N, M, pf, mode=mode, seed=13, ctx=ctx)
+        res = mc_asia_result(100, 100, .04, .3, 1.0, N, M, pf, mode=mode, seed=13, use_cv=True,
+                             ctx=ctx)
         s = _asia_twin(orc, 100, 100, .04, .3, 1.0, N, M, pf, mode, 13)
         for k in range(5):
             if s[k] == 0:
@@ -155,7 +168,7 @@ def test_basket_matches_fp64_twin(orc, ctx, d):
     corr = [1.0 if i == j else .3 for i in range(d) for j in range(d)]
     N = 20000
     res = mc_basket_result(S0, sig, corr, .03, 1.0, 100.0, N, 1, scale_by_sqrt_T=True, seed=11,
-                           ctx=ctx)
+                           use_cv=True, ctx=ctx)
     s = (C.c_double * 5)()
     A = C.c_double * d
     orc.twin_mc_basket(d, A(*S0), A(*sig), (C.c_double * (d * d))(*_chol(corr, d)), .03, 1.0, 1.0,
