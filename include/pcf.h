@@ -152,6 +152,31 @@ PCF_API int pcf_binom_embar(pcf_ctx* ctx, double S0, double E, double r, double 
 PCF_API int pcf_binom_embar_batch(pcf_ctx* ctx, int n, const pcf_binom_contract* contracts,
                                   int mode, double* prices);
 
+/* European option, single-step GBM Monte Carlo, with no memory allocation.
+ * Has no counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc while pricing, such as a plugin hosted by a framework whose
+ * caching allocator already holds the GPU's memory, a latency-critical loop
+ * that cannot afford the device synchronisation cudaMalloc/cudaFree may
+ * cause, or code that may allocate only at start-up. Same paths, same Philox
+ * stream and same sums as pcf_mc_eur with use_cv = 1 (stream id 0).
+ *   - The caller passes the inputs and a device buffer d_sums of 5 doubles,
+ *     which receives {sum y, sum y^2, sum S_T, sum S_T^2, sum y S_T};
+ *     price = exp(-rT) * d_sums[0] / N.
+ *   - Work is queued on `stream` (a cudaStream_t, NULL for the legacy
+ *     default stream); the call does not wait for it.
+ *   - Scratch lives in one fixed device array inside the library (640 KiB per
+ *     GPU that loads it, held until the process exits). N is limited to 2^30
+ *     paths; larger N returns PCF_EINVAL.
+ *   - The first call on each device looks up that array's device address
+ *     and the SM count; make that first call before any stream capture.
+ *   - All calls share the array, so calls whose kernels overlap on the GPU
+ *     (concurrent streams, other host threads) race and must be serialised
+ *     by the caller.
+ *   - It calls no cudaMalloc, cudaFree or other allocating routine. */
+PCF_API int pcf_mc_eur_noalloc(double S0, double E, double r, double sigma, double T,
+                               long long N, int payoff_fun, unsigned long long seed,
+                               double* d_sums, void* stream);
+
 /* ---- Batched pricing -----------------------------------------------------
  * The reference prices one contract per process run (one main() per price).
  * A batch prices many contracts of mixed methods, uneven path and step

@@ -305,3 +305,112 @@ int mc_max_active_blocks(McMethod m, int max_d) {
 }
 
 }  // namespace pcf
+
+// ---- European Monte Carlo that allocates nothing ---------------------------
+//
+// Some callers cannot call cudaMalloc at pricing time. Examples: a plugin
+// inside a framework whose caching allocator has already reserved the GPU's
+// memory; a latency-critical loop where cudaMalloc/cudaFree would stall the
+// device; code certified to allocate only at start-up. pcf_mc_eur_noalloc
+// serves them. It is the European kernel above with its scratch (per-item
+// partial sums and the completion ticket) in a fixed, file-scope device array
+// that is part of the library's device image. Every GPU that loads the library
+// holds the array until the process exits.
+
+#include <mutex>
+
+#include "pcf_api_internal.h"
+
+namespace pcf {
+
+namespace {
+
+constexpr int kNoAllocMaxItems = 16384;  // work items one call may use
+constexpr size_t kNoAllocTicketBytes = 256;
+constexpr size_t kNoAllocBytes =
+    kNoAllocTicketBytes + (size_t)kNoAllocMaxItems * kMoments * sizeof(float2);  // 640.25 KiB
+// A work item covers at most 256 threads x 64 path quads, so 16384 items
+// bound N at 2^30 paths.
+constexpr long long kNoAllocMaxPaths = (long long)kNoAllocMaxItems * kBlock * 64 * 4;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+__global__ void __launch_bounds__(kBlock) mc_eur_noalloc_kernel(McContract C,
+                                                                unsigned char* scratch,
+                                                                double* out) {
+  __shared__ DF sh[32 * kMoments];
+  unsigned* ticket = (unsigned*)scratch;
+  float2* partial = (float2*)(scratch + kNoAllocTicketBytes);
+  const int j = blockIdx.x;
+  Moments<true> mo;
+  eur_item<true>(C, j, mo);
+  DF v[kMoments] = {df_of(mo.y), df_of(mo.yy), df_of(mo.g), df_of(mo.gg), df_of(mo.yg)};
+  DF tot[kMoments];
+  block_sum_df<kMoments>(v, sh, tot);
+  grid_finalize_df<kMoments>(tot, partial, ticket, out, C.items, j);
+}
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices];
+int g_noalloc_sms[kNoAllocMaxDevices];
+
+// Per-device set-up, done once with the device current: the device address
+// of the scratch array (host code must not use the symbol itself) and the SM
+// count that sizes the launch.
+int noalloc_setup(int dev, unsigned char** addr, int* sms) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    int st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch),
+                         "cudaGetSymbolAddress(no-alloc scratch)");
+    if (st) return st;
+    int n = 0;
+    st = cuda_status(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev),
+                     "cudaDeviceGetAttribute");
+    if (st) return st;
+    g_noalloc_sms[dev] = n;
+    g_noalloc_addr[dev] = (unsigned char*)p;
+  }
+  *addr = g_noalloc_addr[dev];
+  *sms = g_noalloc_sms[dev];
+  return PCF_OK;
+}
+
+}  // namespace
+
+}  // namespace pcf
+
+extern "C" int pcf_mc_eur_noalloc(double S0, double E, double r, double sigma, double T,
+                                  long long N, int payoff_fun, unsigned long long seed,
+                                  double* d_sums, void* stream) {
+  using namespace pcf;
+  if (!d_sums) return set_error(PCF_EINVAL, "d_sums is NULL");
+  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+  if (st) return st;
+  if (N > kNoAllocMaxPaths)
+    return set_error(PCF_EINVAL,
+                     "N = %lld exceeds the no-allocation limit of %lld paths (the fixed "
+                     "scratch holds %d work items)",
+                     N, (long long)kNoAllocMaxPaths, kNoAllocMaxItems);
+  int dev = 0;
+  st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st) return st;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return set_error(PCF_EINVAL, "device %d beyond the no-allocation table", dev);
+  unsigned char* scratch = nullptr;
+  int sms = 0;
+  st = noalloc_setup(dev, &scratch, &sms);
+  if (st) return st;
+  pcf_ctx shape;  // only its SM count is read: it sizes the work items
+  shape.sm_count = sms;
+  const McContract C = make_eur(&shape, S0, E, r, sigma, T, N, payoff_fun, seed, 0);
+  if (C.items > kNoAllocMaxItems)
+    return set_error(PCF_EINVAL, "N = %lld needs %d work items; the fixed scratch holds %d", N,
+                     C.items, kNoAllocMaxItems);
+  cudaStream_t s = (cudaStream_t)stream;
+  st = cuda_status(cudaMemsetAsync(scratch, 0, sizeof(unsigned), s), "memset no-alloc ticket");
+  if (st) return st;
+  mc_eur_noalloc_kernel<<<C.items, kBlock, 0, s>>>(C, scratch, d_sums);
+  return cuda_status(cudaGetLastError(), "no-alloc kernel launch");
+}
