@@ -1,33 +1,46 @@
 """Throughput benchmark of the GB300 pricing engine.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME]
+                    [--workload NAME] [--no-cpu]
 
 Prints one JSON line (rank 0). A step is one pass of the engine over one
-batch of synthetic pricing requests (--workload):
+batch of synthetic pricing requests (--workload; parcompfin_gb300/workloads.py
+builds the request sets):
 
-  eur   European calls, the single-step GBM Monte Carlo of the reference's
-        mc_eur (src/mc_eur.cpp:5-27) at the config-0 contract (S0=K=100,
-        r=0.05, sigma=0.2, T=1), 2^28 paths per step, seed 42.
+  eur     config 0: European call S0=K=100 r=.05 sigma=.2 T=1 (mc_eur,
+          src/mc_eur.cpp:5-27), 2^28 paths per step.
+  asia    config 3: 256 Asian calls, M in {12,52,252}, N log-uniform in
+          2^16..2^22 (mc_asia, src/mc_asia.cpp:5-40), one persistent launch,
+          geometric control variate.
+  basket  config 2: baskets of 4, 16, 64 assets, 2^22 paths each
+          (mc_eur_multi, src/mc_eur_multi.cpp:6-35).
+  lsm     American put by Longstaff-Schwartz, N = 2^20 paths, 50 dates
+          (mc_amer, src/mc_amer.cpp:5-114).
+  binom   config 1: 1024 closed-binomial contracts, N uneven in 1e3..2e5
+          (binom_embar, src/binom_embar.cpp:5-50), reference rounding order.
 
-value      paths/s with the request tables already resident in HBM: kernels
-           only, timed with CUDA events on the engine's stream, per step.
-e2e        the same paths/s through the public C ABI (pcf_price_batch) from
-           host parameters to host results, copies included, wall clock.
-roofline   the dominant kernel against its compute bound.
-cpu_baseline  the reference's own CPU code (oracle/_ref when it was compiled
-           on this machine, else the oracle's restatement of it) on all host
-           cores, on a bounded sample of the same workload.
---impl reference runs only that CPU arm and prints its line.
+value         units/s with the request tables already on the device, timed with
+              CUDA events on the engine's stream around each step, L2 flushed
+              between steps (outside the events).
+e2e           the same units/s through the public C ABI from host parameters to
+              host results (copies included), wall clock.
+roofline      the dominant kernel against its bound (SFU for the path
+              generators, HBM for the LSM path matrix).
+cpu_baseline  the reference's OpenMP code on all host cores (oracle/_ref where
+              the reference was compiled on this machine, else the oracle's
+              restatement of the same loops), on a bounded sample.
+--impl reference prints that CPU arm alone.
 
-Multi-GPU (torchrun): every rank prices its own copy of the batch on its own
-GPU with its own Philox streams (weak scaling, no collective on the data
-path); value = all ranks' paths / the slowest rank's time.
+Multi-GPU (torchrun): every rank prices its own copy of the batch with its own
+Philox streams (weak scaling, no collective on the data path); value = all
+ranks' units / the slowest rank's time.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,6 +54,15 @@ sys.path.insert(0, ROOT)
 L2_FLUSH_BYTES = 256 << 20  # > the 129 MB L2 of a GB300
 
 
+def _sfu_roofline(sfu_per_unit, units, ms, sms, sm_mhz):
+    peak = sms * 16 * sm_mhz * 1e6 / 1e9  # G MUFU ops/s: 16 per SM per clock
+    ach = sfu_per_unit * units / (ms * 1e-3) / 1e9
+    return {"bound": "sfu", "achieved": ach, "peak": peak, "unit": "G SFU op/s",
+            "frac": ach / peak, "traffic": None,
+            "peak_source": f"{sms} SMs x 16 MUFU/clk x {sm_mhz:.0f} MHz (median SM clock "
+                           "under load); compute-bound kernel, no HBM traffic to speak of"}
+
+
 # --------------------------------------------------------------------------
 # workloads
 # --------------------------------------------------------------------------
@@ -49,27 +71,42 @@ class EurWorkload:
     metric = "MC paths/sec (European GBM, config-0 contract)"
     unit = "paths/s"
     paths = 1 << 28
-    # Per path: 3 SFU ops (1/2 lg2 + 1/2 sqrt + 1/2 sin + 1/2 cos + 1 ex2).
-    sfu_per_unit = 3.0
+    dominant = "mc_kernel<0,...> (European)"
 
-    def __init__(self, rank: int):
-        self.rank = rank
-
-    def requests(self):
+    def __init__(self, rank):
         import parcompfin_gb300 as pcf
-        return [pcf.request("eur", 100.0, 100.0, 0.05, 0.2, 1.0, self.paths, "call", seed=42,
-                            stream=self.rank)]
+        self.reqs = [pcf.request("eur", 100.0, 100.0, 0.05, 0.2, 1.0, self.paths, "call",
+                                 seed=42, stream=rank)]
 
-    def units_per_step(self) -> float:
+    def setup(self, ctx):
+        import parcompfin_gb300 as pcf
+        self.plan = pcf.Plan(self.reqs, ctx=ctx)
+
+    def step(self, ctx):
+        self.plan.launch()
+
+    def finish(self, ctx):
+        r = self.plan.results()
+        return {"price": r[0].price_plain, "std_error": r[0].std_error_plain}
+
+    def e2e(self, ctx):
+        import parcompfin_gb300 as pcf
+        pcf.price_batch(self.reqs, ctx=ctx)
+        from parcompfin_gb300 import _lib
+        return C.sizeof(_lib.McRequest) * len(self.reqs), C.sizeof(_lib.McResult) * len(self.reqs)
+
+    def units(self):
         return float(self.paths)
 
-    def config(self) -> dict:
-        return {"workload": "eur: European call S0=K=100 r=0.05 sigma=0.2 T=1, "
-                            "2^28 paths/step, Philox seed 42",
-                "paths_per_step": self.paths, "contracts_per_step": 1}
+    def config(self):
+        return {"workload": "eur: European call S0=K=100 r=0.05 sigma=0.2 T=1, 2^28 paths/step, "
+                            "Philox seed 42", "paths_per_step": self.paths, "contracts_per_step": 1}
 
-    def cpu_reference(self, threads: int, budget_s: float):
-        """Time the reference's mc_eur_omp (or its restatement) on host cores."""
+    def roofline(self, ms, sms, mhz):
+        # 3 SFU ops per path: 1/2 lg2 + 1/2 sqrt + 1/2 sin + 1/2 cos + 1 ex2
+        return _sfu_roofline(3.0, self.units(), ms, sms, mhz)
+
+    def cpu_reference(self, threads, budget_s):
         from oracle import loader
         ref = loader.load_ref("mc_eur_omp")
         orc = loader.load()
@@ -78,8 +115,7 @@ class EurWorkload:
             run = lambda n: ref(100.0, 100.0, 0.05, 0.2, 1.0, n, 0, 1.0, threads, 42)
         else:
             kind = "port"
-            run = lambda n: orc.ref_mc_eur_omp(100.0, 100.0, 0.05, 0.2, 1.0, n, 1.0, 42,
-                                               threads)
+            run = lambda n: orc.ref_mc_eur_omp(100.0, 100.0, 0.05, 0.2, 1.0, n, 1.0, 42, threads)
         n = 1 << 20
         t0 = time.perf_counter()
         run(n)
@@ -89,11 +125,271 @@ class EurWorkload:
         price = run(n)
         dt = time.perf_counter() - t0
         return {"value": n / dt, "unit": self.unit, "cores": threads, "kind": kind,
-                "sample": f"mc_eur_omp on {n} paths (config-0 contract), price {price:.6f}, "
+                "sample": f"mc_eur_omp on {n} paths of the config-0 contract, price {price:.6f}, "
                           f"{dt:.2f} s"}
 
 
-WORKLOADS = {"eur": EurWorkload}
+class AsiaWorkload:
+    name = "asia"
+    metric = "MC paths/sec (Asian batch, config 3)"
+    unit = "paths/s"
+    dominant = "mc_kernel<1,...> (Asian, persistent)"
+
+    def __init__(self, rank):
+        import parcompfin_gb300 as pcf
+        from parcompfin_gb300 import workloads
+        self.cs = workloads.config3()
+        self.reqs = [pcf.request("asia", c["S0"], c["E"], c["r"], c["sigma"], c["T"], c["N"], "call",
+                                 M=c["M"], mode=0, use_cv=True, seed=13, stream=rank * 4096 + i)
+                     for i, c in enumerate(self.cs)]
+
+    setup = EurWorkload.setup
+    step = EurWorkload.step
+
+    def finish(self, ctx):
+        r = self.plan.results()
+        worst = max(x.std_error_cv / x.price_cv for x in r if x.price_cv > 0)
+        return {"contracts": len(r), "worst_rel_se_cv": worst}
+
+    e2e = EurWorkload.e2e
+
+    def units(self):
+        return float(sum(c["N"] for c in self.cs))
+
+    def path_steps(self):
+        return float(sum(c["N"] * c["M"] for c in self.cs))
+
+    def config(self):
+        return {"workload": "asia: config 3, 256 Asian calls (seed 13), K~U[90,110], "
+                            "sigma~U[.15,.4], T~U[.5,2], M in {12,52,252}, N=2^U[16,22], "
+                            "geometric control variate, one persistent launch",
+                "paths_per_step": self.units(), "path_steps_per_step": self.path_steps(),
+                "contracts_per_step": len(self.cs)}
+
+    def roofline(self, ms, sms, mhz):
+        # 3 SFU ops per path-step (normal: 2, ex2: 1)
+        return _sfu_roofline(3.0, self.path_steps(), ms, sms, mhz)
+
+    def cpu_reference(self, threads, budget_s):
+        from oracle import loader
+        ref = loader.load_ref("mc_asia_omp")
+        orc = loader.load()
+        kind = "reference" if ref is not None else "port"
+        done_paths = done_steps = 0
+        t0 = time.perf_counter()
+        for c in self.cs:
+            n = max(1000, c["N"] // 64)
+            if ref is not None:
+                ref(c["S0"], c["E"], c["r"], c["sigma"], c["T"], n, c["M"], 1.0, threads, 13)
+            else:
+                orc.ref_mc_asia_omp(c["S0"], c["E"], c["r"], c["sigma"], c["T"], n, c["M"], 1.0,
+                                    13, threads)
+            done_paths += n
+            done_steps += n * c["M"]
+            if time.perf_counter() - t0 > budget_s:
+                break
+        dt = time.perf_counter() - t0
+        # Paths per second at this batch's mix of step counts.
+        rate_steps = done_steps / dt
+        value = rate_steps * self.units() / self.path_steps()
+        return {"value": value, "unit": self.unit, "cores": threads, "kind": kind,
+                "sample": f"mc_asia_omp on the config-3 contracts at N/64 ({done_paths} paths, "
+                          f"{done_steps} path-steps, {dt:.2f} s); paths/s scaled to the batch's "
+                          "step mix"}
+
+
+class BasketWorkload:
+    name = "basket"
+    metric = "MC paths/sec (basket, config 2)"
+    unit = "paths/s"
+    dominant = "mc_kernel<2,64,...> (basket)"
+
+    def __init__(self, rank):
+        import parcompfin_gb300 as pcf
+        from parcompfin_gb300 import workloads
+        self.cs = workloads.config2()
+        self.reqs = [pcf.request("basket", 100.0, c["E"], c["r"], 0.2, c["T"], c["N"], "call",
+                                 assets=c["assets"], basket_S0=c["basket_S0"],
+                                 basket_sigma=c["basket_sigma"], corr=c["corr"], use_cv=True,
+                                 scale_by_sqrt_T=True, seed=11, stream=rank * 16 + i)
+                     for i, c in enumerate(self.cs)]
+
+    setup = EurWorkload.setup
+    step = EurWorkload.step
+
+    def finish(self, ctx):
+        r = self.plan.results()
+        return {"prices_cv": [x.price_cv for x in r]}
+
+    e2e = EurWorkload.e2e
+
+    def units(self):
+        return float(sum(c["N"] for c in self.cs))
+
+    def config(self):
+        return {"workload": "basket: config 2, d in {4,16,64}, S0=K=100, r=.03, T=1, "
+                            "sigma_i~U[.15,.35], corr 0.7 equicorr(.3) + 0.3 Wishart(d,d+2) "
+                            "seed 11, 2^22 paths each, geometric-basket control variate",
+                "paths_per_step": self.units(), "contracts_per_step": len(self.cs)}
+
+    def roofline(self, ms, sms, mhz):
+        sfu = sum(c["N"] * 3.0 * c["assets"] for c in self.cs) / self.units()
+        return _sfu_roofline(sfu, self.units(), ms, sms, mhz)
+
+    def cpu_reference(self, threads, budget_s):
+        # The reference's basket needs Eigen and Boost (include/mvn.h), absent
+        # here: time the oracle's FP64 restatement on all cores instead.
+        from oracle import loader
+        orc = loader.load()
+        import numpy as np
+        done = 0
+        t0 = time.perf_counter()
+        for c in self.cs:
+            d = c["assets"]
+            L = np.linalg.cholesky(np.array(c["corr"])).ravel()
+            A = C.c_double * d
+            s = (C.c_double * 5)()
+            n = 1 << 15
+            orc.twin_mc_basket(d, A(*c["basket_S0"]), A(*c["basket_sigma"]),
+                               (C.c_double * (d * d))(*L), c["r"], c["T"], math.sqrt(c["T"]),
+                               c["E"], n, 1, 11, 0, s)
+            done += n
+        dt = time.perf_counter() - t0
+        # Paths of the three contracts come in equal numbers in the batch.
+        return {"value": done / dt, "unit": self.unit, "cores": threads,
+                "kind": "port",
+                "sample": f"oracle FP64 basket restatement (the reference's Eigen/Boost build is "
+                          f"unavailable), 2^15 paths per contract, {dt:.2f} s"}
+
+
+class LsmWorkload:
+    name = "lsm"
+    metric = "MC paths/sec (American put, Longstaff-Schwartz)"
+    unit = "paths/s"
+    N, M = 1 << 20, 50
+    dominant = "lsm_kernel"
+
+    def __init__(self, rank):
+        self.rank = rank
+
+    def setup(self, ctx):
+        pass
+
+    def step(self, ctx):
+        import parcompfin_gb300 as pcf
+        self.res = pcf.mc_amer_result(100.0, 100.0, 0.05, 0.3, 1.0, self.N, self.M, "put",
+                                      seed=1 + self.rank, ctx=ctx)
+
+    def finish(self, ctx):
+        return {"price": self.res.price, "std_error": self.res.std_error}
+
+    def e2e(self, ctx):
+        self.step(ctx)
+        return 4 * (self.M + 1), C.sizeof(C.c_double) * 5 + 16
+
+    def units(self):
+        return float(self.N)
+
+    def config(self):
+        return {"workload": "lsm: American put S0=K=100 r=.05 sigma=.3 T=1, 50 exercise dates, "
+                            "2^20 paths (antithetic), basis {1,x,x^2}",
+                "paths_per_step": self.N, "dates": self.M, "contracts_per_step": 1}
+
+    def roofline(self, ms, sms, mhz, peaks):
+        alg = 8.0 * self.N * self.M  # one FP32 write + one FP32 read per path-date
+        ach = alg / (ms * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
+                               "fallback 6.8 TB/s"}
+
+    def cpu_reference(self, threads, budget_s):
+        from oracle import loader
+        ref = loader.load_ref("mc_amer_omp")
+        orc = loader.load()
+        n = 1 << 16
+        t0 = time.perf_counter()
+        if ref is not None:
+            kind = "reference"
+            ref(100.0, 100.0, 0.05, 0.3, 1.0, n, self.M, -1.0, threads, 1)
+        else:
+            kind = "port"
+            orc.ref_mc_amer(100.0, 100.0, 0.05, 0.3, 1.0, n, self.M, -1.0, 1)
+            threads = 1
+        dt = time.perf_counter() - t0
+        return {"value": n / dt, "unit": self.unit, "cores": threads, "kind": kind,
+                "sample": f"{'mc_amer_omp' if ref is not None else 'mc_amer (serial port)'} on "
+                          f"{n} paths, 50 dates, {dt:.2f} s"}
+
+
+class BinomWorkload:
+    name = "binom"
+    metric = "contracts/sec (closed binomial sum, config 1)"
+    unit = "contracts/s"
+    dominant = "binom_kernel"
+
+    def __init__(self, rank):
+        from parcompfin_gb300 import workloads
+        self.cs = workloads.config1()
+
+    def setup(self, ctx):
+        pass
+
+    def step(self, ctx):
+        import parcompfin_gb300 as pcf
+        self.prices = pcf.binom_embar_batch(self.cs, mode="reference", ctx=ctx)
+
+    def finish(self, ctx):
+        return {"first_prices": self.prices[:3]}
+
+    def e2e(self, ctx):
+        self.step(ctx)
+        return 48 * len(self.cs), 8 * len(self.cs)
+
+    def units(self):
+        return float(len(self.cs))
+
+    def config(self):
+        return {"workload": "binom: config 1, 1024 contracts (seed 7), K~U[80,120], "
+                            "r~U[.01,.06], sigma~U[.1,.5], T~U[.25,2], call/put 50/50, "
+                            "N~U{1000..200000}, reference rounding order",
+                "contracts_per_step": len(self.cs)}
+
+    def roofline(self, ms, sms, mhz, peaks=None):
+        return {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None,
+                "note": "FP64 and L2-latency bound binary searches over per-binade prefix "
+                        "tables; no HBM or tensor bound applies"}
+
+    def cpu_reference(self, threads, budget_s):
+        from oracle import loader
+        ref = loader.load_ref("binom_embar_omp")
+        orc = loader.load()
+        kind = "reference" if ref is not None else "port"
+        # The full batch is ~25 CPU-hours (O(N^2) per contract). Time contracts
+        # of growing N, fit a * N^2, extrapolate to the batch (labelled).
+        samples = []
+        t_all = time.perf_counter()
+        for N in (1000, 2000, 4000, 8000, 12000):
+            t0 = time.perf_counter()
+            if ref is not None:
+                ref(100.0, 100.0, 0.03, 0.3, 1.0, N, 0, 1.0, threads)
+            else:
+                orc.ref_binom_embar_omp(100.0, 100.0, 0.03, 0.3, 1.0, N, 1.0, threads)
+            samples.append((N, time.perf_counter() - t0))
+            if time.perf_counter() - t_all > budget_s:
+                break
+        a = sum(t * N * N for N, t in samples) / sum(N ** 4 for N, _ in samples)
+        total = sum(a * c[5] ** 2 for c in self.cs)
+        return {"value": len(self.cs) / total, "unit": self.unit, "cores": threads, "kind": kind,
+                "sample": f"binom_embar_omp timed at N in {[n for n, _ in samples]}, fit "
+                          f"t = {a:.3e} N^2 s, extrapolated to the 1024-contract batch "
+                          f"({total / 3600:.1f} h)"}
+
+
+WORKLOADS = {w.name: w for w in (EurWorkload, AsiaWorkload, BasketWorkload, LsmWorkload,
+                                  BinomWorkload)}
 
 
 # --------------------------------------------------------------------------
@@ -126,7 +422,7 @@ class ClockSampler:
         for ln in self.proc.stdout:
             self.lines.append(ln.strip())
 
-    def stop(self) -> dict | None:
+    def stop(self):
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -137,14 +433,18 @@ class ClockSampler:
         rows = [ln.split(", ") for ln in self.lines if ln]
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(r[1]) for r in rows if len(r) > 2) if v is not None]
+        mx = [v for v in (num(r[2]) for r in rows if len(r) > 2) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4)
                           if len(r) > 5 + i and r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows)}
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
 def measured_peaks() -> dict:
@@ -156,10 +456,8 @@ def measured_peaks() -> dict:
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 def run_reference(args, wl_cls):
@@ -168,8 +466,7 @@ def run_reference(args, wl_cls):
         return
     threads = os.cpu_count() or 1
     wl = wl_cls(0)
-    vals = []
-    sample = None
+    vals, sample = [], None
     for i in range(args.warmup + args.steps):
         r = wl.cpu_reference(threads, budget_s=2.0)
         if i >= args.warmup:
@@ -178,10 +475,10 @@ def run_reference(args, wl_cls):
     value = statistics.median(vals)
     line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * wl.units_per_step() / value, "higher_is_better": True,
+            "ms_per_step": 1e3 * wl.units() / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": wl.config(),
-            "cpu_baseline": {"value": value, "unit": wl.unit, "cores": threads,
+            "cpu_baseline": {"value": value, "unit": wl.unit, "cores": sample["cores"],
                              "kind": sample["kind"], "sample": sample["sample"]},
             "e2e": {"value": value, "unit": wl.unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -191,7 +488,6 @@ def run_reference(args, wl_cls):
 def run_ours(args, wl_cls):
     import torch
     import parcompfin_gb300 as pcf
-    from parcompfin_gb300 import _lib
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -204,18 +500,18 @@ def run_ours(args, wl_cls):
     ctx = pcf.Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    reqs = wl.requests()
-    plan = pcf.Plan(reqs, ctx=ctx)
+    wl.setup(ctx)
 
     def barrier():
         torch.cuda.synchronize(dev)
         if ws > 1:
             torch.distributed.barrier()
 
-    # warm-up
+    with torch.cuda.stream(stream):
+        flush.zero_()
     for _ in range(args.warmup):
-        plan.launch()
-    plan.results()
+        wl.step(ctx)
+    check = wl.finish(ctx)
     barrier()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -229,78 +525,64 @@ def run_ours(args, wl_cls):
         for i in range(args.steps):
             flush.zero_()  # evict L2 between steps (outside the step events)
             starts[i].record(stream)
-            plan.launch()
+            wl.step(ctx)
             ends[i].record(stream)
     barrier()
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.launches - l0
-    res = plan.results()
+    check = wl.finish(ctx)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(step_ms) / len(step_ms)
-    # e2e: the public API from host parameters to host results, every step.
-    barrier()
-    e2e_ms = []
-    for i in range(max(3, args.steps)):
-        t0 = time.perf_counter()
-        out = pcf.price_batch(reqs, ctx=ctx)
-        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_ms, io = [], (0, 0)
+    if not args.no_e2e:
+        barrier()
+        for _ in range(max(3, args.steps)):
+            t0 = time.perf_counter()
+            io = wl.e2e(ctx)
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
     clk = clocks.stop()
-    e2e_med = statistics.median(e2e_ms)
+    e2e_med = statistics.median(e2e_ms) if e2e_ms else float("nan")
     if ws > 1:
         t = torch.tensor([ms, e2e_med], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms, e2e_med = float(t[0]), float(t[1])
-    units = wl.units_per_step() * ws
+    units = wl.units() * ws
     value = units / (ms * 1e-3)
-    e2e_value = units / (e2e_med * 1e-3)
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
     peaks = measured_peaks()
     sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    props = torch.cuda.get_device_properties(dev)
-    sfu_peak = props.multi_processor_count * 16 * sm_mhz * 1e6 / 1e9  # G SFU ops/s
-    sfu_ach = wl.sfu_per_unit * wl.units_per_step() / (ms * 1e-3) / 1e9
-    h2d = len(reqs) * C_SIZEOF_REQUEST
-    d2h = len(reqs) * C_SIZEOF_RESULT
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    try:
+        roof = wl.roofline(ms, sms, sm_mhz, peaks)
+    except TypeError:
+        roof = wl.roofline(ms, sms, sm_mhz)
+    roof["kernel"] = wl.dominant
     line = {
         "metric": wl.metric, "value": value, "unit": wl.unit, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 paths, f64 sums", "data": "synthetic",
-        "config": dict(wl.config(), l2="flushed: 256 MiB write between steps, "
-                                       "outside the per-step CUDA events",
+        "dtype": "f32 paths, f64 sums" if wl.name != "binom" else "f64", "data": "synthetic",
+        "config": dict(wl.config(), l2="flushed: 256 MiB write between steps, outside the "
+                                       "per-step CUDA events",
                        wall_ms_per_step=1e3 * t_wall / args.steps),
-        "roofline": {"bound": "sfu", "achieved": sfu_ach, "peak": sfu_peak,
-                     "unit": "G SFU op/s", "frac": sfu_ach / sfu_peak, "traffic": None,
-                     "peak_source": f"{props.multi_processor_count} SMs x 16 MUFU/clk x "
-                                    f"{sm_mhz:.0f} MHz (median SM clock under load)"},
-        "e2e": {"value": e2e_value, "unit": wl.unit, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_med},
+        "roofline": roof,
+        "e2e": {"value": units / (e2e_med * 1e-3) if e2e_ms else None, "unit": wl.unit,
+                "h2d_bytes_per_step": io[0], "d2h_bytes_per_step": io[1], "ms_per_step": e2e_med},
         "gpu_launches": launches,
         "clocks": clk,
-        "check": {"price": res[0].price_plain, "std_error": res[0].std_error_plain},
+        "check": check,
     }
-    if rank == 0:
-        threads = os.cpu_count() or 1
+    if not args.no_cpu:
         try:
-            line["cpu_baseline"] = wl.cpu_reference(threads, budget_s=10.0)
+            line["cpu_baseline"] = wl.cpu_reference(os.cpu_count() or 1, budget_s=10.0)
         except Exception as e:  # noqa: BLE001
             line["cpu_baseline"] = {"error": repr(e)}
     print(json.dumps(line), flush=True)
-    plan.close()
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
-
-
-def _sizes():
-    from parcompfin_gb300 import _lib
-    import ctypes as C
-    return C.sizeof(_lib.McRequest), C.sizeof(_lib.McResult)
-
-
-C_SIZEOF_REQUEST, C_SIZEOF_RESULT = _sizes()
 
 
 def main():
@@ -310,8 +592,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="eur", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "ours":
+        args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)
