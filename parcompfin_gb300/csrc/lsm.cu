@@ -34,9 +34,13 @@
 #include <algorithm>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "pcf_api_internal.h"
 #include "pcf_device.cuh"
 #include "pcf_math.h"
+
+namespace cg = cooperative_groups;
 
 namespace pcf {
 
@@ -147,16 +151,24 @@ __device__ __forceinline__ void reg_accumulate(const LsmParams& P, float Sv, flo
   acc[7] = fmaf(y, x2, acc[7]);
 }
 
-// Block reduction of the regression sums for date m, publication of the
-// block's partial, the bounded group barrier, the grid reduction (every block
-// sums all partials in block order, so all blocks get the same bits) and the
-// 3x3 solve. Leaves the date's mode and coefficients in shared memory. When
-// `next_row` >= 0, thread 0 issues the bulk copy of that row into `next_buf`
-// once every thread is past the slice that buffer held. Returns false if the
-// barrier wait gave up.
+// Block reduction of the regression sums for date m, the exchange of block
+// partials, the 3x3 solve, and the issue of the next bulk copy.
+//   cooperative launch (CLUSTER = false): each block publishes its partial in
+//     global memory, waits at the bounded group barrier, then every block
+//     sums all partials in block order (so all blocks get the same bits);
+//   cluster launch (CLUSTER = true, one cluster per contract): each CTA keeps
+//     its partial in shared memory; after a hardware cluster barrier every
+//     CTA reads all CTAs' partials through distributed shared memory, in
+//     rank order.
+// Leaves the date's mode and coefficients in shared memory. When `next_row`
+// >= 0, thread 0 issues the bulk copy of that row into `next_buf` once every
+// thread is past the slice that buffer held. Returns false if a bounded wait
+// gave up (cooperative launch only).
+template <bool CLUSTER>
 __device__ bool lsm_regress(const LsmParams& P, const LsmSmem& S, float (&acc)[kRegSums], int m,
-                            int b, DF* sh, double* s_coef, int* s_mode, int next_row, long long p0,
-                            int nbr, int PB, float* next_buf, uint64_t* next_bar) {
+                            int b, DF* sh, DF (*red)[kRegSums], double* s_coef, int* s_mode,
+                            int next_row, long long p0, int nbr, int PB, float* next_buf,
+                            uint64_t* next_bar) {
   DF v[kRegSums], tot[kRegSums];
 #pragma unroll
   for (int q = 0; q < kRegSums; ++q) v[q] = DF{acc[q], 0.f};
@@ -164,24 +176,39 @@ __device__ bool lsm_regress(const LsmParams& P, const LsmSmem& S, float (&acc)[k
   float2* slot = (float2*)P.partial + (size_t)(m & 1) * P.nblocks * kRegSums;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int q = 0; q < kRegSums; ++q) slot[(size_t)b * kRegSums + q] = make_float2(tot[q].hi, tot[q].lo);
+    for (int q = 0; q < kRegSums; ++q) {
+      if (CLUSTER) red[m & 1][q] = tot[q];
+      else slot[(size_t)b * kRegSums + q] = make_float2(tot[q].hi, tot[q].lo);
+    }
     if (next_row >= 0 && nbr > 0) issue_row(P, S, next_row, p0, nbr, PB, next_buf, next_bar);
   }
-  if (!group_barrier(P.barrier, (unsigned)P.nblocks, P.err, P.wait_limit)) return false;
+  if (CLUSTER) {
+    cg::this_cluster().sync();
+  } else {
+    if (!group_barrier(P.barrier, (unsigned)P.nblocks, P.err, P.wait_limit)) return false;
+  }
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     DF g[kRegSums];
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) g[q] = DF{0.f, 0.f};
-    for (int bb = lane; bb < P.nblocks; bb += 32) {
-      const float4* r4 = (const float4*)(slot + (size_t)bb * kRegSums);
-      float4 a[4];
+    if (CLUSTER) {
+      if (lane < P.nblocks) {
+        const DF* rr = cg::this_cluster().map_shared_rank(&red[m & 1][0], lane);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = __ldcg(r4 + u);
+        for (int q = 0; q < kRegSums; ++q) g[q] = rr[q];
+      }
+    } else {
+      for (int bb = lane; bb < P.nblocks; bb += 32) {
+        const float4* r4 = (const float4*)(slot + (size_t)bb * kRegSums);
+        float4 a[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        g[2 * u] = df_add(g[2 * u], DF{a[u].x, a[u].y});
-        g[2 * u + 1] = df_add(g[2 * u + 1], DF{a[u].z, a[u].w});
+        for (int u = 0; u < 4; ++u) a[u] = __ldcg(r4 + u);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          g[2 * u] = df_add(g[2 * u], DF{a[u].x, a[u].y});
+          g[2 * u + 1] = df_add(g[2 * u + 1], DF{a[u].z, a[u].w});
+        }
       }
     }
     double t[kRegSums];
@@ -231,17 +258,23 @@ __device__ __forceinline__ void lsm_update(const LsmParams& P, const LsmSmem& S,
   }
 }
 
-__global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
+// One contract's forward pass, backward sweep and final moments, executed by
+// block `b` of the contract's `P.nblocks` blocks. In a cluster launch a
+// failed copy wait is recorded and the CTA keeps taking part in every cluster
+// barrier (a hardware barrier has no timeout), so no CTA leaves early.
+template <bool CLUSTER>
+__device__ void lsm_body(const LsmParams& P, int b) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int PB = P.pairs_per_block;
   const int M = P.M;
   const LsmSmem S = carve(smem_raw, PB, M);
   __shared__ DF sh[32 * kRegSums];
+  __shared__ DF red[2][kRegSums];
+  __shared__ DF fin[kMoments];
   __shared__ double s_coef[3];
   __shared__ int s_mode;  // 0 skip date, 1 few ITM paths, 2 regression
   __shared__ int s_ok;
 
-  const int b = blockIdx.x;
   const long long p0 = (long long)b * PB;
   const int nb = (int)max(0LL, min((long long)PB, P.H - p0));  // pairs in this block
   const int nbr = (nb + 3) & ~3;                                // bulk-copy width
@@ -302,7 +335,7 @@ __global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
     }
   }
   __syncthreads();
-  alive = s_ok != 0;
+  if (!CLUSTER) alive = s_ok != 0;
 
   // Sums for date M-1 (the only date without a preceding update pass).
   if (alive) {
@@ -319,8 +352,8 @@ __global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
       }
     }
     if (threadIdx.x == 0 && M - 2 >= 1 && nbr > 0) pending[1] = true;  // issued in lsm_regress
-    alive = lsm_regress(P, S, acc, M - 1, b, sh, s_coef, &s_mode, M - 2 >= 1 ? M - 3 : -1, p0,
-                        nbr, PB, S.buf[1], &S.bar[1]);
+    alive = lsm_regress<CLUSTER>(P, S, acc, M - 1, b, sh, red, s_coef, &s_mode,
+                                 M - 2 >= 1 ? M - 3 : -1, p0, nbr, PB, S.buf[1], &S.bar[1]);
   }
 
   // Date m: update with date m's coefficients, fused with the sums of date m-1.
@@ -336,7 +369,7 @@ __global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
         }
       }
       __syncthreads();
-      if (!s_ok) {
+      if (!s_ok && !CLUSTER) {
         alive = false;
         break;
       }
@@ -364,8 +397,8 @@ __global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
     // date m-2 goes there.
     const int next_row = m - 2 >= 1 ? m - 3 : -1;
     if (threadIdx.x == 0 && next_row >= 0 && nbr > 0) pending[k] = true;
-    alive = lsm_regress(P, S, acc, m - 1, b, sh, s_coef, &s_mode, next_row, p0, nbr, PB,
-                        S.buf[k], &S.bar[k]);
+    alive = lsm_regress<CLUSTER>(P, S, acc, m - 1, b, sh, red, s_coef, &s_mode, next_row, p0,
+                                 nbr, PB, S.buf[k], &S.bar[k]);
   }
   __syncthreads();
   if (!alive) {
@@ -395,7 +428,38 @@ __global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
   DF v[kMoments] = {df_of(sy), df_of(syy), df_of(sg), df_of(sgg), df_of(syg)};
   DF tot[kMoments];
   block_sum_df<kMoments>(v, sh, tot);
-  grid_finalize_df<kMoments>(tot, (float2*)P.fpartial, P.ticket, P.out, P.nblocks, b);
+  if (CLUSTER) {
+    if (threadIdx.x == 0)
+      for (int q = 0; q < kMoments; ++q) fin[q] = tot[q];
+    cg::this_cluster().sync();
+    if (b == 0 && threadIdx.x == 0) {
+      DF t[kMoments];
+      for (int q = 0; q < kMoments; ++q) t[q] = DF{0.f, 0.f};
+      for (int r = 0; r < P.nblocks; ++r) {
+        const DF* rf = cg::this_cluster().map_shared_rank(&fin[0], r);
+        for (int q = 0; q < kMoments; ++q) t[q] = df_add(t[q], rf[q]);
+      }
+      for (int q = 0; q < kMoments; ++q) P.out[q] = df_value(t[q]);
+    }
+    cg::this_cluster().sync();  // rank 0 has read every CTA's shared memory
+  } else {
+    grid_finalize_df<kMoments>(tot, (float2*)P.fpartial, P.ticket, P.out, P.nblocks, b);
+  }
+}
+
+__global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
+  lsm_body<false>(P, blockIdx.x);
+}
+
+// Many contracts in one launch, one thread-block cluster per contract
+// (cluster size = the contracts' common block count).
+__global__ void __launch_bounds__(kLsmBlock) lsm_cluster_kernel(const LsmParams* __restrict__ cs) {
+  __shared__ LsmParams sP;  // the contract's parameters, read from shared memory
+  const unsigned rank = cg::this_cluster().block_rank();
+  const int c = (int)(blockIdx.x / cg::this_cluster().num_blocks());
+  if (threadIdx.x == 0) sP = cs[c];
+  __syncthreads();
+  lsm_body<true>(sP, (int)rank);
 }
 
 size_t lsm_smem(int PB, int M) {
@@ -405,7 +469,286 @@ size_t lsm_smem(int PB, int M) {
 
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Parameters of one contract that do not depend on where its buffers live.
+void lsm_fill(LsmParams& P, double S0, double E, double r, double sigma, double T, long long N,
+              int M, int pf, int ref_exercise, unsigned long long seed, unsigned stream) {
+  const double log2e = 1.4426950408889634;
+  const double dtd = T / M;
+  memset(&P, 0, sizeof P);
+  P.pf = (float)pf;
+  P.nK = (float)(-pf * E);
+  P.E = (float)E;
+  P.invE = (float)(1.0 / E);
+  P.a2 = (float)((r - 0.5 * sigma * sigma) * dtd * log2e);
+  P.b2 = (float)(sigma * sqrt(dtd) * log2e);
+  P.l2S0 = (float)(log(S0) * log2e);
+  P.gdisc = (float)exp(-r * T);
+  P.M = M;
+  P.ref_exercise = ref_exercise ? 1 : 0;
+  P.H = N / 2;
+  P.Hp = (P.H + 3) & ~3LL;
+  P.seed_lo = (uint32_t)seed;
+  P.seed_hi = (uint32_t)(seed >> 32);
+  P.stream = stream;
+  P.wait_limit = 1u << 22;       // ~64 ns sleep + an L2 round trip per poll: seconds
+  P.copy_wait_limit = 1u << 20;  // try_wait polls: far beyond a microsecond-scale copy
+}
+
+void dtab_fill(float* dst, double r, double T, int M) {
+  const double dtd = T / M;
+  for (int k = 0; k <= M; ++k) dst[k] = (float)exp(-r * dtd * k);
+}
+
+constexpr size_t kStaticSmemReserve = 4096;  // lsm_body's static shared arrays
+
+// Cooperative-launch grid for one contract: at most one block per SM, at
+// least one pair per thread. Returns false if it cannot be co-resident.
+bool coop_shape(const pcf_ctx* c, long long H, int M, int& G, int& PB, size_t& smem) {
+  const long long G0 = std::max(1LL, std::min((H + kLsmBlock - 1) / kLsmBlock,
+                                              (long long)c->sm_count));
+  PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
+  G = (int)((H + PB - 1) / PB);
+  smem = lsm_smem(PB, M);
+  return smem + kStaticSmemReserve <= kLsmMaxSmem;
+}
+
 }  // namespace
+
+int check_lsm_request(double S0, double E, double r, double sigma, double T, long long N, int M,
+                      int pf) {
+  int st = check_common(S0, E, r, sigma, T, N, pf);
+  if (st) return st;
+  if (N % 2 != 0)  // include/common.h:180
+    return set_error(PCF_EINVAL, "N needs to be divisible by 2 for finding paths");
+  if (M < 2 || M > 4096) return set_error(PCF_EINVAL, "M must be in [2, 4096]");
+  if (!(E > 0)) return set_error(PCF_EINVAL, "E must be > 0 for the LSM regression basis");
+  return PCF_OK;
+}
+
+void fill_amer_result(const double* s, long long N, double S0, double E, double r, double sigma,
+                      double T, int pf, bool use_cv, pcf_mc_result* out) {
+  fill_result(s, N, bs_price(S0, E, r, sigma, T, pf), 1.0, use_cv, out);
+  // src/mc_amer.cpp:113: the price is at least the immediate exercise value.
+  const double intrinsic = std::max(pf * (S0 - E), 0.0);
+  out->price = std::max(out->price, intrinsic);
+  out->price_plain = std::max(out->price_plain, intrinsic);
+  if (use_cv) out->price_cv = std::max(out->price_cv, intrinsic);
+}
+
+// ---- batches of American contracts (used by pcf_plan_*) ----
+
+struct LsmCluster {  // one cluster launch: every contract with the same shape
+  int CL = 0, PB = 0, C = 0;
+  size_t smem = 0;
+  LsmParams* d_params = nullptr;
+};
+
+struct LsmBatch {
+  std::vector<LsmCluster> clusters;
+  std::vector<LsmParams> coop;  // contracts too large for one cluster
+  std::vector<int> coop_grid;
+  std::vector<size_t> coop_smem;
+  void* d_mem = nullptr;
+  size_t bytes = 0;
+};
+
+int lsm_cluster_size(pcf_ctx* c) {
+  // 16 CTAs per cluster where the device can co-schedule them, else 8.
+  static int cached = 0;
+  if (cached) return cached;
+  cudaFuncSetAttribute(lsm_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  const size_t smem = lsm_smem(8192, 64);
+  cudaFuncSetAttribute(lsm_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 16;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(16);
+  cfg.blockDim = dim3(kLsmBlock);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, lsm_cluster_kernel, &cfg) == cudaSuccess && n > 0)
+    cached = 16;
+  else
+    cached = 8;
+  cudaGetLastError();
+  (void)c;
+  return cached;
+}
+
+int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmBatch** out) {
+  *out = nullptr;
+  LsmBatch* B = new LsmBatch();
+  const int CL = lsm_cluster_size(c);
+  const int kPB[] = {512, 1024, 2048, 4096, 8192};
+  // Assign shapes.
+  std::vector<int> cls(reqs.size(), -1);  // index into kPB, or -1 for cooperative
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    const long long H = reqs[i].N / 2;
+    for (int k = 0; k < 5; ++k)
+      if ((long long)CL * kPB[k] >= H &&
+          lsm_smem(kPB[k], reqs[i].M) + kStaticSmemReserve <= kLsmMaxSmem) {
+        cls[i] = k;
+        break;
+      }
+  }
+  // Device layout: params tables | dtabs | path matrices | coop scratch.
+  std::vector<LsmParams> host;
+  std::vector<std::vector<int>> members(5);
+  for (size_t i = 0; i < reqs.size(); ++i)
+    if (cls[i] >= 0) members[cls[i]].push_back((int)i);
+  size_t off = 0;
+  std::vector<size_t> o_params(5, 0);
+  for (int k = 0; k < 5; ++k) {
+    o_params[k] = off;
+    off = a256(off + sizeof(LsmParams) * members[k].size());
+  }
+  std::vector<size_t> o_dt(reqs.size()), o_paths(reqs.size()), o_coop(reqs.size(), 0);
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    o_dt[i] = off;
+    off = a256(off + sizeof(float) * (reqs[i].M + 1));
+  }
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    o_paths[i] = off;
+    const long long Hp = ((reqs[i].N / 2) + 3) & ~3LL;
+    off = a256(off + sizeof(float) * (size_t)reqs[i].M * 2 * (size_t)Hp);
+  }
+  std::vector<int> coop_G(reqs.size(), 0), coop_PB(reqs.size(), 0);
+  std::vector<size_t> coop_sm(reqs.size(), 0);
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    if (cls[i] >= 0) continue;
+    if (!coop_shape(c, reqs[i].N / 2, reqs[i].M, coop_G[i], coop_PB[i], coop_sm[i])) {
+      delete B;
+      return set_error(PCF_EINVAL, "American request with N = %lld is too large", reqs[i].N);
+    }
+    o_coop[i] = off;  // partial (2 G 8 float2) | fpartial (G 5 float2) | 2 counters
+    off = a256(off + 8 * (2 * (size_t)coop_G[i] * kRegSums + (size_t)coop_G[i] * kMoments) + 16);
+  }
+  if (c->budget_bytes && off > c->budget_bytes) {
+    delete B;
+    return set_error(PCF_ENOMEM, "American batch needs %zu device bytes, over the budget", off);
+  }
+  int st = cuda_status(cudaMalloc(&B->d_mem, std::max(off, (size_t)256)), "cudaMalloc(LSM batch)");
+  if (st) {
+    delete B;
+    return st;
+  }
+  B->bytes = off;
+  char* d = (char*)B->d_mem;
+  std::vector<char> h(off, 0);
+  auto fill = [&](size_t i, LsmParams& P) {
+    const LsmRequest& q = reqs[i];
+    lsm_fill(P, q.S0, q.E, q.r, q.sigma, q.T, q.N, q.M, q.pf, q.ref_exercise, q.seed, q.stream);
+    dtab_fill((float*)&h[o_dt[i]], q.r, q.T, q.M);
+    P.dtab = (const float*)(d + o_dt[i]);
+    P.paths = (float*)(d + o_paths[i]);
+    P.out = q.d_out;
+    P.err = q.d_flags;
+    P.singular = q.d_flags + 1;
+  };
+  for (int k = 0; k < 5; ++k) {
+    if (members[k].empty()) continue;
+    LsmCluster L;
+    L.CL = CL;
+    L.PB = kPB[k];
+    L.C = (int)members[k].size();
+    int Mmax = 2;
+    LsmParams* tab = (LsmParams*)&h[o_params[k]];
+    for (int j = 0; j < L.C; ++j) {
+      const int i = members[k][j];
+      fill(i, tab[j]);
+      tab[j].pairs_per_block = L.PB;
+      tab[j].nblocks = CL;
+      Mmax = std::max(Mmax, reqs[i].M);
+    }
+    L.smem = lsm_smem(L.PB, Mmax);
+    L.d_params = (LsmParams*)(d + o_params[k]);
+    B->clusters.push_back(L);
+  }
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    if (cls[i] >= 0) continue;
+    LsmParams P;
+    fill(i, P);
+    P.pairs_per_block = coop_PB[i];
+    P.nblocks = coop_G[i];
+    char* base = d + o_coop[i];
+    P.partial = (double*)base;
+    P.fpartial = (double*)(base + 8 * 2 * (size_t)coop_G[i] * kRegSums);
+    unsigned* cnt = (unsigned*)(base + 8 * (2 * (size_t)coop_G[i] * kRegSums +
+                                            (size_t)coop_G[i] * kMoments));
+    P.barrier = cnt;
+    P.ticket = cnt + 1;
+    B->coop.push_back(P);
+    B->coop_grid.push_back(coop_G[i]);
+    B->coop_smem.push_back(coop_sm[i]);
+  }
+  st = cuda_status(cudaMemcpyAsync(d, h.data(), off, cudaMemcpyHostToDevice, c->stream),
+                   "H2D LSM batch");
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "LSM batch upload");
+  if (st) {
+    lsm_batch_destroy(B);
+    return st;
+  }
+  *out = B;
+  return PCF_OK;
+}
+
+int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
+  int st;
+  for (const LsmCluster& L : B->clusters) {
+    st = cuda_status(cudaFuncSetAttribute(lsm_cluster_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)L.smem),
+                     "lsm cluster smem attribute");
+    if (st) return st;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = L.CL;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(L.C * L.CL);
+    cfg.blockDim = dim3(kLsmBlock);
+    cfg.dynamicSmemBytes = L.smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    st = cuda_status(cudaLaunchKernelEx(&cfg, lsm_cluster_kernel,
+                                        (const LsmParams*)L.d_params),
+                     "lsm cluster launch");
+    if (st) return st;
+    c->launches += 1;
+  }
+  for (size_t i = 0; i < B->coop.size(); ++i) {
+    LsmParams& P = B->coop[i];
+    st = cuda_status(cudaMemsetAsync(P.barrier, 0, 2 * sizeof(unsigned), s), "memset LSM counters");
+    if (st) return st;
+    st = cuda_status(cudaFuncSetAttribute(lsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)B->coop_smem[i]),
+                     "lsm smem attribute");
+    if (st) return st;
+    void* args[] = {&P};
+    st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_kernel, dim3(B->coop_grid[i]),
+                                                 dim3(kLsmBlock), args, B->coop_smem[i], s),
+                     "lsm cooperative launch");
+    if (st) return st;
+    c->launches += 1;
+  }
+  return PCF_OK;
+}
+
+int lsm_batch_kernels(const LsmBatch* B) { return (int)(B->clusters.size() + B->coop.size()); }
+
+void lsm_batch_destroy(LsmBatch* B) {
+  if (!B) return;
+  if (B->d_mem) cudaFree(B->d_mem);
+  delete B;
+}
 
 }  // namespace pcf
 
@@ -415,26 +758,13 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
                            long long N, int M, int payoff_fun, int ref_exercise,
                            unsigned long long seed, int use_cv, pcf_mc_result* out) {
   if (!out) return set_error(PCF_EINVAL, "out is NULL");
-  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+  int st = check_lsm_request(S0, E, r, sigma, T, N, M, payoff_fun);
   if (st) return st;
-  if (N % 2 != 0)  // include/common.h:180
-    return set_error(PCF_EINVAL, "N needs to be divisible by 2 for finding paths");
-  if (M < 2 || M > 4096) return set_error(PCF_EINVAL, "M must be in [2, 4096]");
-  if (!(E > 0)) return set_error(PCF_EINVAL, "E must be > 0 for the LSM regression basis");
   pcf_ctx* c = resolve_ctx(ctx, &st);
   if (!c) return st;
-  const long long H = N / 2;
-  const long long Hp = (H + 3) & ~3LL;
-
-  // Grid: one block per SM at most (each block reduces every partial, so
-  // fewer, fatter blocks are cheaper), at least one pair per thread, all
-  // blocks co-resident (the cooperative launch checks this too).
-  const long long G0 = std::max(1LL, std::min((H + kLsmBlock - 1) / kLsmBlock,
-                                              (long long)c->sm_count));
-  const int PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
-  const int G = (int)((H + PB - 1) / PB);
-  const size_t smem = lsm_smem(PB, M);
-  if (smem > kLsmMaxSmem)
+  int G = 0, PB = 0;
+  size_t smem = 0;
+  if (!coop_shape(c, N / 2, M, G, PB, smem))
     return set_error(PCF_EINVAL, "N = %lld is too large for one device sweep", N);
   st = cuda_status(cudaFuncSetAttribute(lsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem),
@@ -447,8 +777,12 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if ((long long)occ * c->sm_count < G)
     return set_error(PCF_EINVAL, "LSM grid of %d blocks cannot be co-resident", G);
 
+  LsmParams P;
+  lsm_fill(P, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, 0);
+  P.pairs_per_block = PB;
+  P.nblocks = G;
   // Resident path matrix: M rows x 2*Hp floats.
-  const size_t paths_bytes = sizeof(float) * (size_t)M * 2 * (size_t)Hp;
+  const size_t paths_bytes = sizeof(float) * (size_t)M * 2 * (size_t)P.Hp;
   if (paths_bytes > c->paths_cap) {
     if (c->d_paths) cudaFree(c->d_paths);
     c->d_paths = nullptr;
@@ -471,36 +805,12 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if (st) return st;
   char* d = (char*)c->d_buf;
   char* h = (char*)c->h_buf;
-  const double dtd = T / M;
-  for (int k = 0; k <= M; ++k) ((float*)(h + o_dt))[k] = (float)exp(-r * dtd * k);
+  dtab_fill((float*)(h + o_dt), r, T, M);
   st = cuda_status(cudaMemcpyAsync(d + o_dt, h + o_dt, sizeof(float) * (M + 1),
                                    cudaMemcpyHostToDevice, c->stream), "H2D dtab");
   if (!st) st = cuda_status(cudaMemsetAsync(d + o_cnt, 0, sizeof(unsigned) * 4, c->stream),
                             "memset counters");
   if (st) return st;
-
-  const double log2e = 1.4426950408889634;
-  LsmParams P;
-  memset(&P, 0, sizeof P);
-  P.pf = (float)payoff_fun;
-  P.nK = (float)(-payoff_fun * E);
-  P.E = (float)E;
-  P.invE = (float)(1.0 / E);
-  P.a2 = (float)((r - 0.5 * sigma * sigma) * dtd * log2e);
-  P.b2 = (float)(sigma * sqrt(dtd) * log2e);
-  P.l2S0 = (float)(log(S0) * log2e);
-  P.gdisc = (float)exp(-r * T);
-  P.M = M;
-  P.ref_exercise = ref_exercise ? 1 : 0;
-  P.H = H;
-  P.Hp = Hp;
-  P.pairs_per_block = PB;
-  P.nblocks = G;
-  P.seed_lo = (uint32_t)seed;
-  P.seed_hi = (uint32_t)(seed >> 32);
-  P.stream = 0;
-  P.wait_limit = 1u << 22;       // ~64 ns sleep + an L2 round trip per poll: seconds
-  P.copy_wait_limit = 1u << 20;  // try_wait polls: far beyond a microsecond-scale copy
   P.paths = (float*)c->d_paths;
   P.dtab = (const float*)(d + o_dt);
   P.partial = (double*)(d + o_part);
@@ -527,11 +837,6 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if (flags[3])
     return set_error(PCF_ESINGULAR, "Detereminant is not > 0 at %d exercise date(s)", flags[3]);
   const double* s = (const double*)(h + o_out);
-  fill_result(s, N, bs_price(S0, E, r, sigma, T, payoff_fun), 1.0, use_cv != 0, out);
-  // src/mc_amer.cpp:113: the price is at least the immediate exercise value.
-  const double intrinsic = std::max(payoff_fun * (S0 - E), 0.0);
-  out->price = std::max(out->price, intrinsic);
-  out->price_plain = std::max(out->price_plain, intrinsic);
-  if (use_cv) out->price_cv = std::max(out->price_cv, intrinsic);
+  fill_amer_result(s, N, S0, E, r, sigma, T, payoff_fun, use_cv != 0, out);
   return PCF_OK;
 }

@@ -53,4 +53,24 @@ int make_basket(int d, const double* S0, const double* sig, const double* corr, 
                 double T, double E, long long N, int pf, double ts, unsigned long long seed,
                 uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g);
 
+// American (Longstaff-Schwartz) contracts in a batch (lsm.cu).
+struct LsmRequest {
+  double S0, E, r, sigma, T;
+  long long N;
+  int M, pf, ref_exercise;
+  unsigned long long seed;
+  unsigned stream;
+  double* d_out;   // kMoments sums, device
+  int* d_flags;    // {wait gave up, singular dates}, device, zeroed before a launch
+};
+struct LsmBatch;
+int check_lsm_request(double S0, double E, double r, double sigma, double T, long long N, int M,
+                      int pf);
+void fill_amer_result(const double* s, long long N, double S0, double E, double r, double sigma,
+                      double T, int pf, bool use_cv, pcf_mc_result* out);
+int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmBatch** out);
+int lsm_batch_launch(pcf_ctx* c, LsmBatch* b, cudaStream_t s);
+int lsm_batch_kernels(const LsmBatch* b);
+void lsm_batch_destroy(LsmBatch* b);
+
 }  // namespace pcf

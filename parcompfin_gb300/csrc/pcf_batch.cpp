@@ -47,6 +47,14 @@ struct pcf_plan {
   unsigned* d_tickets = nullptr;
   size_t tickets_bytes = 0;
   double* d_out = nullptr;
+  // American requests: priced by an LSM batch; two flag words each (wait gave
+  // up, singular dates) live in the ticket region, so the per-launch memset
+  // clears them.
+  LsmBatch* lsm = nullptr;
+  std::vector<int> amer;              // request indices
+  std::vector<pcf_mc_request> amer_q; // their parameters (for the estimators)
+  int* d_amer_flags = nullptr;
+  int* h_amer_flags = nullptr;
 };
 
 static int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContract& k,
@@ -118,6 +126,19 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
   g[2].method = MC_BASKET;
   for (int i = 0; i < n; ++i) {
     const int m = reqs[i].method;
+    if (m == PCF_METHOD_AMER) {
+      const pcf_mc_request& q = reqs[i];
+      st = check_lsm_request(q.S0, q.E, q.r, q.sigma, q.T, q.N, q.M, q.payoff_fun);
+      if (st) {
+        delete p;
+        return set_error(st, "request %d: %s", i, pcf_last_error());
+      }
+      p->amer.push_back(i);
+      p->amer_q.push_back(q);
+      p->npaths[i] = q.N;
+      p->use_cv[i] = q.use_cv != 0;
+      continue;
+    }
     if (m < 0 || m > 2) {
       delete p;
       return set_error(PCF_EINVAL, "request %d: method %d not supported in a batch", i, m);
@@ -177,6 +198,8 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
     ticket_words += (size_t)C + 1;
   }
   const size_t o_tickets = off;
+  const size_t amer_flag_word = ticket_words;
+  ticket_words += 2 * p->amer.size();
   p->tickets_bytes = sizeof(unsigned) * ticket_words;
   off = a256(off + p->tickets_bytes);
   const size_t o_out = off;
@@ -187,7 +210,8 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
   }
   st = cuda_status(cudaMalloc(&p->d_mem, off), "cudaMalloc(plan)");
   if (!st) st = cuda_status(cudaMallocHost((void**)&p->h_out,
-                                           sizeof(double) * kMoments * std::max(n, 1)),
+                                           sizeof(double) * kMoments * std::max(n, 1) +
+                                               sizeof(int) * 2 * (p->amer.size() + 1)),
                             "cudaMallocHost(plan)");
   if (st) {
     pcf_plan_destroy(p);
@@ -232,6 +256,35 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
       return st;
     }
   }
+  if (!p->amer.empty()) {
+    p->d_amer_flags = (int*)(p->d_tickets + amer_flag_word);
+    p->h_amer_flags = (int*)(p->h_out + (size_t)kMoments * std::max(n, 1));
+    std::vector<LsmRequest> lr;
+    for (size_t a = 0; a < p->amer.size(); ++a) {
+      const pcf_mc_request& q = p->amer_q[a];
+      LsmRequest x;
+      x.S0 = q.S0;
+      x.E = q.E;
+      x.r = q.r;
+      x.sigma = q.sigma;
+      x.T = q.T;
+      x.N = q.N;
+      x.M = q.M;
+      x.pf = q.payoff_fun;
+      x.ref_exercise = q.mode;
+      x.seed = q.seed;
+      x.stream = q.stream;
+      x.d_out = p->d_out + (size_t)row * kMoments;
+      x.d_flags = p->d_amer_flags + 2 * a;
+      p->out_slot[p->amer[a]] = row++;
+      lr.push_back(x);
+    }
+    st = lsm_batch_create(c, lr, &p->lsm);
+    if (st) {
+      pcf_plan_destroy(p);
+      return st;
+    }
+  }
   *out = p;
   return PCF_OK;
 }
@@ -251,10 +304,13 @@ int pcf_plan_launch(pcf_plan* p) {
     if (st) return st;
     c->launches += 1;
   }
+  if (p->lsm) return lsm_batch_launch(c, p->lsm, c->stream);
   return PCF_OK;
 }
 
-int pcf_plan_kernel_count(const pcf_plan* p) { return p ? (int)p->groups.size() : 0; }
+int pcf_plan_kernel_count(const pcf_plan* p) {
+  return p ? (int)p->groups.size() + (p->lsm ? lsm_batch_kernels(p->lsm) : 0) : 0;
+}
 
 int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
   if (!p || (p->n && !results)) return set_error(PCF_EINVAL, "bad arguments");
@@ -264,18 +320,40 @@ int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
   int st = cuda_status(cudaMemcpyAsync(p->h_out, p->d_out, sizeof(double) * kMoments * p->n,
                                        cudaMemcpyDeviceToHost, c->stream),
                        "D2H batch results");
+  if (!st && !p->amer.empty())
+    st = cuda_status(cudaMemcpyAsync(p->h_amer_flags, p->d_amer_flags,
+                                     sizeof(int) * 2 * p->amer.size(), cudaMemcpyDeviceToHost,
+                                     c->stream),
+                     "D2H American flags");
   if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "batch kernels");
   if (st) return st;
   for (int i = 0; i < p->n; ++i)
     fill_result(p->h_out + (size_t)p->out_slot[i] * kMoments, p->npaths[i], p->mu_g[i],
                 p->disc[i], p->use_cv[i] != 0, &results[i]);
-  return PCF_OK;
+  int status = PCF_OK;
+  for (size_t a = 0; a < p->amer.size(); ++a) {
+    const pcf_mc_request& q = p->amer_q[a];
+    const int i = p->amer[a];
+    fill_amer_result(p->h_out + (size_t)p->out_slot[i] * kMoments, q.N, q.S0, q.E, q.r, q.sigma,
+                     q.T, q.payoff_fun, q.use_cv != 0, &results[i]);
+    const int* fl = p->h_amer_flags + 2 * a;
+    if (fl[0] || fl[1]) {
+      // A request whose sweep failed gets NaN; the call reports the first failure.
+      results[i].price = results[i].price_plain = results[i].price_cv = NAN;
+      if (status == PCF_OK)
+        status = set_error(fl[0] ? PCF_ETIMEOUT : PCF_ESINGULAR,
+                           "request %d: %s", i, fl[0] ? "LSM device wait gave up"
+                                                      : "Detereminant is not > 0");
+    }
+  }
+  return status;
 }
 
 int pcf_plan_destroy(pcf_plan* p) {
   if (!p) return PCF_OK;
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
+  lsm_batch_destroy(p->lsm);
   if (p->d_mem) cudaFree(p->d_mem);
   if (p->h_out) cudaFreeHost(p->h_out);
   delete p;
