@@ -388,8 +388,233 @@ class BinomWorkload:
                           f"({total / 3600:.1f} h)"}
 
 
-WORKLOADS = {w.name: w for w in (EurWorkload, AsiaWorkload, BasketWorkload, LsmWorkload,
-                                  BinomWorkload)}
+class MixedWorkload:
+    """Config 4: the served mixed stream at a fixed relative standard error."""
+    name = "mixed"
+    metric = ("MC paths/sec at fixed std-error (5e-4 of price), mixed request stream; "
+              "p50/p99 latency served")
+    unit = "paths/s"
+    dominant = "lsm_cluster_kernel (American, one cluster per contract)"
+    R = 1000             # requests per step
+    TARGET = 5e-4        # relative standard error
+    LOADS = (1000, 10000, 50000)
+
+    def __init__(self, rank):
+        import parcompfin_gb300 as pcf
+        from parcompfin_gb300 import workloads
+        self.rank = rank
+        self.spec = workloads.config4(self.R, seed=17 + 1000 * rank)
+        self.base = [self._req(pcf, s, 0) for s in self.spec]
+
+    @staticmethod
+    def _req(pcf, s, N, use_cv=True):
+        kw = dict(use_cv=use_cv, seed=4242, stream=s["id"])
+        if s["kind"] == "eur":
+            return pcf.request("eur", s["S0"], s["E"], s["r"], s["sigma"], s["T"], N or 4, "call", **kw)
+        if s["kind"] == "asia":
+            return pcf.request("asia", s["S0"], s["E"], s["r"], s["sigma"], s["T"], N or 4, "call",
+                               M=s["M"], **kw)
+        if s["kind"] == "basket":
+            return pcf.request("basket", s["S0"], s["E"], s["r"], s["sigma"], s["T"], N or 4, "call",
+                               assets=s["assets"], rho=s["rho"], basket_sigma=s["basket_sigma"],
+                               scale_by_sqrt_T=True, **kw)
+        return pcf.request("amer", s["S0"], s["E"], s["r"], s["sigma"], s["T"], N or 2, "put",
+                           M=s["M"], **kw)
+
+    def setup(self, ctx):
+        import parcompfin_gb300 as pcf
+        # Pilot (outside the timed region): each request's path count at the
+        # target standard error, for the control-variate estimator (the engine)
+        # and the plain one (the one-contract-per-launch baseline).
+        pilot = [dict(q, N=(1 << 14)) for q in self.base]
+        res = pcf.price_batch(pilot, ctx=ctx)
+        self.N, self.N_plain = [], []
+        for q, r in zip(self.base, res):
+            n0 = 1 << 14
+            def need(se, price):
+                if not (se > 0 and price > 0):
+                    return n0
+                return int(min(1 << 40, max(n0, 1.05 * se * se * n0 / (self.TARGET * price) ** 2)))
+            n_cv = need(r.std_error_cv, abs(r.price_cv))
+            n_pl = need(r.std_error_plain, abs(r.price_plain))
+            if q["method"] == 3:
+                n_cv = min(max(n_cv, 1 << 16), 1 << 21) // 2 * 2
+                n_pl = min(max(n_pl, 1 << 16), 1 << 21) // 2 * 2
+            else:
+                n_cv = min(n_cv, 1 << 26)
+                n_pl = min(n_pl, 1 << 28)
+            self.N.append(n_cv)
+            self.N_plain.append(n_pl)
+        self.main = [dict(q, N=n) for q, n in zip(self.base, self.N)]
+        self.plan = pcf.Plan(self.main, ctx=ctx)
+        self.amer_idx = [i for i, q in enumerate(self.main) if q["method"] == 3]
+        self.amer_plan = pcf.Plan([self.main[i] for i in self.amer_idx], ctx=ctx)
+
+    def step(self, ctx):
+        self.plan.launch()
+
+    def finish(self, ctx):
+        res = self.plan.results()
+        rel = sorted(r.std_error / r.price for r in res if r.price > 0 and r.std_error == r.std_error)
+        return {"requests": len(res), "median_rel_se": rel[len(rel) // 2], "max_rel_se": rel[-1],
+                "paths_per_step": self.units()}
+
+    def e2e(self, ctx):
+        import parcompfin_gb300 as pcf
+        out, stats = pcf.serve_trace(self.base, [0.0] * len(self.base), target_rel_se=self.TARGET,
+                                     ctx=ctx)
+        self.e2e_stats = stats
+        return (C.sizeof(pcf._lib.McRequest) * len(self.base),
+                C.sizeof(pcf._lib.ServedResult) * len(self.base))
+
+    def e2e_units(self):
+        return float(self.e2e_stats.paths)
+
+    def units(self):
+        return float(sum(self.N))
+
+    def contracts(self):
+        return float(len(self.N))
+
+    def config(self):
+        kinds = {}
+        for s in self.spec:
+            kinds[s["kind"]] = kinds.get(s["kind"], 0) + 1
+        return {"workload": "mixed: config 4, 1000 requests per step (seed 17): 30% European "
+                            "(config-0 jittered), 20% basket d~U{2..32}, 30% Asian (config-3 "
+                            "distribution), 20% American put (LSM, 50 dates, N in 2^16..2^21); "
+                            "each priced to a 5e-4 relative standard error with its control "
+                            "variate",
+                "requests_per_step": self.R, "kinds": kinds, "target_rel_se": self.TARGET,
+                "paths_per_step": self.units() if hasattr(self, "N") else None}
+
+    def roofline(self, ms, sms, mhz, peaks):
+        import torch
+        # The American sub-plan alone, timed the same way: HBM bytes of its path
+        # matrices (8 B per path-date) over its kernel time.
+        s = torch.cuda.ExternalStream(self.ctx_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        self.amer_plan.launch()
+        times = []
+        for _ in range(3):
+            e0.record(s)
+            self.amer_plan.launch()
+            e1.record(s)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        t = min(times)
+        alg = sum(8.0 * self.main[i]["N"] * self.main[i]["M"] for i in self.amer_idx)
+        ach = alg / (t * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": None, "kernel_ms": t,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
+                               "fallback 6.8 TB/s",
+                "share_of_step": t / ms}
+
+    def extra(self, ctx):
+        """Served latency at offered loads, and the plain one-contract-per-launch path."""
+        import parcompfin_gb300 as pcf
+        from parcompfin_gb300 import workloads
+        served = {}
+        for rate in self.LOADS:
+            n = int(min(4 * self.R, max(self.R, rate * 1.0)))
+            spec = workloads.config4(n, seed=29 + rate)
+            reqs = [self._req(pcf, s, 0) for s in spec]
+            arr = workloads.poisson_arrivals(n, rate, seed=31 + rate)
+            out, st = pcf.serve_trace(reqs, arr, target_rel_se=self.TARGET, ctx=ctx)
+            served[str(rate)] = {"offered_per_s": rate, "requests": n, "p50_ms": st.p50_ms,
+                                 "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
+                                 "contracts_per_s": st.contracts_per_s,
+                                 "paths_per_s": st.paths_per_s, "batches": st.batches}
+        # Plain path: each request alone, plain estimator, at the path count the
+        # plain estimator needs for the same standard error.
+        k = min(60, len(self.spec))
+        t0 = time.perf_counter()
+        paths = 0
+        for i in range(k):
+            q = self.base[i]
+            N = self.N_plain[i]
+            paths += N
+            if q["method"] == 0:
+                pcf.mc_eur_result(q["S0"], q["E"], q["r"], q["sigma"], q["T"], N, q["payoff_fun"],
+                                  seed=7, ctx=ctx)
+            elif q["method"] == 1:
+                pcf.mc_asia_result(q["S0"], q["E"], q["r"], q["sigma"], q["T"], N, q["M"],
+                                   q["payoff_fun"], seed=7, ctx=ctx)
+            elif q["method"] == 2:
+                s = self.spec[i]
+                pcf.mc_basket_result([q["S0"]] * s["assets"], s["basket_sigma"],
+                                     [1.0 if a == b else s["rho"] for a in range(s["assets"])
+                                      for b in range(s["assets"])], q["r"], q["T"], q["E"], N,
+                                     q["payoff_fun"], seed=7, ctx=ctx)
+            else:
+                pcf.mc_amer_result(q["S0"], q["E"], q["r"], q["sigma"], q["T"], N, q["M"],
+                                   q["payoff_fun"], seed=7, ctx=ctx)
+        dt = time.perf_counter() - t0
+        plain = {"contracts_per_s": k / dt, "paths_per_s": paths / dt, "sample_requests": k,
+                 "note": "each request alone through its single-contract entry point, plain "
+                         "estimator, at the path count the plain estimator needs for the same "
+                         "5e-4 relative standard error (American capped at 2^21)"}
+        return {"served": served, "plain_gpu": plain}
+
+    def cpu_reference(self, threads, budget_s):
+        from oracle import loader
+        orc = loader.load()
+        refs = {k: loader.load_ref(k) for k in ("mc_eur_omp", "mc_asia_omp", "mc_amer_omp")}
+        kind = "reference" if all(refs.values()) else "port"
+        t0 = time.perf_counter()
+        paths = 0
+        done = 0
+        for s in self.spec:
+            n = 1 << 15 if s["kind"] in ("eur", "basket") else 1 << 13
+            if s["kind"] == "eur":
+                if refs["mc_eur_omp"]:
+                    refs["mc_eur_omp"](s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, 0, 1.0,
+                                       threads, 1)
+                else:
+                    orc.ref_mc_eur_omp(s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, 1.0, 1,
+                                       threads)
+            elif s["kind"] == "asia":
+                if refs["mc_asia_omp"]:
+                    refs["mc_asia_omp"](s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"], 1.0,
+                                        threads, 1)
+                else:
+                    orc.ref_mc_asia_omp(s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"], 1.0,
+                                        1, threads)
+            elif s["kind"] == "basket":
+                # No Eigen/Boost build of the reference basket here: the oracle's
+                # FP64 restatement on all cores stands in.
+                import numpy as np
+                d = s["assets"]
+                corr = np.full((d, d), s["rho"])
+                np.fill_diagonal(corr, 1.0)
+                L = np.linalg.cholesky(corr).ravel()
+                A = C.c_double * d
+                sums = (C.c_double * 5)()
+                orc.twin_mc_basket(d, A(*([s["S0"]] * d)), A(*s["basket_sigma"]),
+                                   (C.c_double * (d * d))(*L), s["r"], s["T"], math.sqrt(s["T"]),
+                                   s["E"], n, 1, 1, 0, sums)
+            else:
+                if refs["mc_amer_omp"]:
+                    refs["mc_amer_omp"](s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"],
+                                        -1.0, threads, 1)
+                else:
+                    orc.ref_mc_amer(s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"], -1.0, 1)
+            paths += n
+            done += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+        dt = time.perf_counter() - t0
+        return {"value": paths / dt, "unit": self.unit, "cores": threads, "kind": kind,
+                "ms_per_step": 1e3 * dt,
+                "sample": f"the reference's OpenMP pricers (basket: oracle restatement) on the first "
+                          f"{done} requests of the mix, 2^15 paths (European, basket) or 2^13 "
+                          f"(Asian, American) each: {paths} paths in {dt:.2f} s"}
+
+
+WORKLOADS = {w.name: w for w in (MixedWorkload, EurWorkload, AsiaWorkload, BasketWorkload,
+                                  LsmWorkload, BinomWorkload)}
 
 
 # --------------------------------------------------------------------------
@@ -473,9 +698,12 @@ def run_reference(args, wl_cls):
             vals.append(r["value"])
             sample = r
     value = statistics.median(vals)
+    ms_step = sample.get("ms_per_step")
+    if ms_step is None:
+        ms_step = 1e3 * wl.units() / value
     line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * wl.units() / value, "higher_is_better": True,
+            "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": wl.config(),
             "cpu_baseline": {"value": value, "unit": wl.unit, "cores": sample["cores"],
@@ -498,6 +726,7 @@ def run_ours(args, wl_cls):
     torch.cuda.set_device(dev)
     wl = wl_cls(rank)
     ctx = pcf.Context(dev)
+    wl.ctx_stream = ctx.stream
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     wl.setup(ctx)
@@ -548,6 +777,7 @@ def run_ours(args, wl_cls):
         ms, e2e_med = float(t[0]), float(t[1])
     units = wl.units() * ws
     value = units / (ms * 1e-3)
+    e2e_units = (wl.e2e_units() if hasattr(wl, "e2e_units") else wl.units()) * ws
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
@@ -568,15 +798,23 @@ def run_ours(args, wl_cls):
                                        "per-step CUDA events",
                        wall_ms_per_step=1e3 * t_wall / args.steps),
         "roofline": roof,
-        "e2e": {"value": units / (e2e_med * 1e-3) if e2e_ms else None, "unit": wl.unit,
+        "e2e": {"value": e2e_units / (e2e_med * 1e-3) if e2e_ms else None, "unit": wl.unit,
                 "h2d_bytes_per_step": io[0], "d2h_bytes_per_step": io[1], "ms_per_step": e2e_med},
         "gpu_launches": launches,
         "clocks": clk,
         "check": check,
     }
+    if hasattr(wl, "contracts"):
+        line["contracts_per_s"] = wl.contracts() * ws / (ms * 1e-3)
+    if hasattr(wl, "extra") and not args.no_e2e:
+        line.update(wl.extra(ctx))
+        if "plain_gpu" in line and "contracts_per_s" in line:
+            line["plain_gpu"]["engine_over_plain_contracts"] = (
+                line["contracts_per_s"] / line["plain_gpu"]["contracts_per_s"])
     if not args.no_cpu:
         try:
             line["cpu_baseline"] = wl.cpu_reference(os.cpu_count() or 1, budget_s=10.0)
+            line["cpu_baseline"].pop("ms_per_step", None)
         except Exception as e:  # noqa: BLE001
             line["cpu_baseline"] = {"error": repr(e)}
     print(json.dumps(line), flush=True)
@@ -591,7 +829,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="eur", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
     args = ap.parse_args()

@@ -224,6 +224,54 @@ PCF_API int pcf_plan_destroy(pcf_plan* plan);
 PCF_API int pcf_price_batch(pcf_ctx* ctx, int n, const pcf_mc_request* reqs,
                             pcf_mc_result* results);
 
+/* ---- Serving ---------------------------------------------------------------
+ * A continuous-batching loop. Requests arrive over time; every request whose
+ * arrival time has passed is admitted into the next free batch slot. Slots
+ * have device memory reserved up front, sized from the free HBM, so nothing is
+ * allocated while serving. Several slots are in flight on their own streams,
+ * so a batch admitted while others run overlaps with them on the device.
+ * With target_rel_se > 0, each request is priced to that relative standard
+ * error: a pilot run estimates the variance of its estimator (the
+ * control-variate one when use_cv is set), and the main run uses the path
+ * count that reaches the target, clamped to [pilot_paths, max_paths]
+ * (American: [2^16, max_amer_paths], even). The reference has no serving
+ * layer: its runscript_*.sh launch one process per price. */
+typedef struct pcf_server_config {
+  double target_rel_se;     /* <= 0: price each request at its own N, no pilot */
+  long long pilot_paths;    /* 0: 2^14 */
+  long long max_paths;      /* 0: 2^26 */
+  long long max_amer_paths; /* 0: 2^21 */
+  int max_batch;            /* requests per batch; 0: 2048 */
+  int slots;                /* batches in flight; 0: 3 */
+  double hbm_fraction;      /* share of free device memory reserved; 0: 0.5 */
+} pcf_server_config;
+
+typedef struct pcf_served_result {
+  pcf_mc_result result;
+  double arrival_s;   /* trace time the request arrived */
+  double admit_s;     /* when it entered a batch */
+  double done_s;      /* when its price was on the host */
+  long long paths;    /* paths simulated for it (pilot + main) */
+  int status;         /* PCF_OK or the error of its batch */
+} pcf_served_result;
+
+typedef struct pcf_server_stats {
+  int completed;
+  int batches;
+  double wall_s;          /* first arrival to last completion */
+  double p50_ms, p99_ms, mean_ms, max_ms;   /* arrival -> done */
+  double contracts_per_s;
+  double paths_per_s;
+  long long paths;
+  size_t reserved_bytes;  /* device memory the loop reserved */
+} pcf_server_stats;
+
+/* Replays a request trace (arrival_s non-decreasing, seconds from the start)
+ * against the wall clock and serves it; fills out[n] and stats. */
+PCF_API int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg, int n,
+                            const pcf_mc_request* reqs, const double* arrival_s,
+                            pcf_served_result* out, pcf_server_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -492,6 +492,18 @@ ORC_EXPORT double ref_binom_vanilla_amer(double S0, double E, double r, double s
   return v[0];
 }
 
+namespace {
+/* Black-Scholes price with time `rem` to expiry (rem = 0: the payoff). */
+double bs_rem(double S, double E, double r, double sigma, double rem, int pf) {
+  if (rem <= 0) return payoff(S, E, pf);
+  const double sd = sigma * sqrt(rem), dK = E * exp(-r * rem);
+  if (sd <= 0) return std::max(pf * (S - dK), 0.0);
+  const double d1 = (log(S / E) + (r + 0.5 * sigma * sigma) * rem) / sd, d2 = d1 - sd;
+  if (pf == 1) return S * norm_cdf(d1) - dK * norm_cdf(d2);
+  return dK * norm_cdf(-d2) - S * norm_cdf(-d1);
+}
+}  // namespace
+
 /* ------------------------------------------------------------------------ */
 /* 2. FP64 twins of the GPU kernels (identical Philox draws)                */
 /* ------------------------------------------------------------------------ */
@@ -597,7 +609,11 @@ ORC_EXPORT void twin_mc_basket(int d, const double* S0, const double* sig, const
  * <= 2 ITM paths: exercise where the exercise value beats y (src/mc_amer.cpp:75-83).
  * Exercise value: payoff(S) by default; with ref_exercise = 1 it is the
  * reference's payoff(S - E, E) (src/mc_amer.cpp:100).
- * out[0..4] moment sums of y = disc. cash flow, g = exp(-rT) payoff(S_M);
+ * out[0..4] moment sums over the N/2 antithetic pairs of the pair means of
+ * y = the discounted cash flow and g = the control variate:
+ *   g = exp(-r tau dt) * P_E(S_tau, T - tau dt), the discounted Black-Scholes
+ *       price at the exercise date (a martingale, so E[g] = P_E(S0, T));
+ *   with ref_exercise = 1: g = exp(-rT) payoff(S_M);
  * out[5] = 1 if a regression was singular. */
 ORC_EXPORT void twin_mc_amer(double S0, double E, double r, double sigma, double T, int64_t N,
                              int M, int pf, int ref_exercise, uint64_t seed, uint32_t stream,
@@ -659,9 +675,15 @@ ORC_EXPORT void twin_mc_amer(double S0, double E, double r, double sigma, double
   }
   double s[5] = {0, 0, 0, 0, 0};
   const double dT = exp(-r * T);
-  for (int64_t n = 0; n < N; ++n) {
-    const double y = cf[n] * disc[tau[n]];
-    const double g = dT * payoff(S[(size_t)M * N + n], E, pf);
+  auto cv = [&](int64_t n) {
+    if (ref_exercise) return dT * payoff(S[(size_t)M * N + n], E, pf);
+    const int t = tau[n];
+    if (t == M) return disc[M] * cf[n];
+    return disc[t] * bs_rem(S[(size_t)t * N + n], E, r, sigma, (M - t) * dt, pf);
+  };
+  for (int64_t p = 0; p < H; ++p) {
+    const double y = 0.5 * (cf[p] * disc[tau[p]] + cf[p + H] * disc[tau[p + H]]);
+    const double g = 0.5 * (cv(p) + cv(p + H));
     s[0] += y; s[1] += y * y; s[2] += g; s[3] += g * g; s[4] += y * g;
   }
   for (int k = 0; k < 5; ++k) out[k] = s[k];

@@ -10,6 +10,7 @@ from .api import (  # noqa: F401
     binom_embar,
     binom_embar_batch,
     price_batch,
+    serve_trace,
     request,
     mc_amer,
     mc_amer_result,

@@ -78,6 +78,28 @@ class McRequest(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("target_rel_se", C.c_double), ("pilot_paths", C.c_longlong),
+                ("max_paths", C.c_longlong), ("max_amer_paths", C.c_longlong),
+                ("max_batch", C.c_int), ("slots", C.c_int), ("hbm_fraction", C.c_double)]
+
+
+class ServedResult(C.Structure):
+    _fields_ = [("result", McResult), ("arrival_s", C.c_double), ("admit_s", C.c_double),
+                ("done_s", C.c_double), ("paths", C.c_longlong), ("status", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int), ("batches", C.c_int), ("wall_s", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("max_ms", C.c_double), ("contracts_per_s", C.c_double),
+                ("paths_per_s", C.c_double), ("paths", C.c_longlong),
+                ("reserved_bytes", C.c_size_t)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BinomContract(C.Structure):
     _fields_ = [("S0", C.c_double), ("E", C.c_double), ("r", C.c_double),
                 ("sigma", C.c_double), ("T", C.c_double), ("N", C.c_int),
@@ -118,6 +140,8 @@ SIGNATURES = {
     "pcf_plan_kernel_count": (_I, [_P]),
     "pcf_plan_destroy": (_I, [_P]),
     "pcf_price_batch": (_I, [_P, _I, C.POINTER(McRequest), C.POINTER(McResult)]),
+    "pcf_serve_trace": (_I, [_P, C.POINTER(ServerConfig), _I, C.POINTER(McRequest), _PD,
+                             C.POINTER(ServedResult), C.POINTER(ServerStats)]),
 }
 
 _lock = threading.Lock()

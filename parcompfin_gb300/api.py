@@ -236,6 +236,24 @@ class Plan:
         self.close()
 
 
+def serve_trace(reqs, arrivals, *, target_rel_se=5e-4, pilot_paths=1 << 14, max_paths=1 << 26,
+                max_amer_paths=1 << 21, max_batch=2048, slots=3, hbm_fraction=0.5, ctx=None):
+    """Serve request() dicts arriving at `arrivals` (seconds, non-decreasing)
+    with the continuous-batching loop; returns (per-request ServedResult list,
+    ServerStats)."""
+    lib = _lib.load()
+    arr, keep = _pack(reqs)
+    t = (C.c_double * len(reqs))(*map(float, arrivals))
+    cfg = _lib.ServerConfig(float(target_rel_se), int(pilot_paths), int(max_paths),
+                            int(max_amer_paths), int(max_batch), int(slots), float(hbm_fraction))
+    out = (_lib.ServedResult * len(reqs))()
+    stats = _lib.ServerStats()
+    st = lib.pcf_serve_trace(_h(ctx), C.byref(cfg), len(reqs), arr, t, out, C.byref(stats))
+    if st not in (_lib.PCF_OK, _lib.PCF_ESINGULAR):
+        _lib.check(st)
+    return list(out), stats
+
+
 def price_batch(reqs, ctx=None):
     """Price a list of request() dicts in one call; returns McResult per request."""
     lib = _lib.load()

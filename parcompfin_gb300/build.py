@@ -31,6 +31,7 @@ SOURCES = [
     ("binom.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("pcf_api.cpp", []),
     ("pcf_batch.cpp", []),
+    ("pcf_server.cpp", []),
     ("pcf_math.cpp", []),
 ]
 

@@ -23,8 +23,10 @@
 //             the same bits), solves the normal equations by the adjugate
 //             formula and updates the exercise decision of its paths from the
 //             same shared-memory slice;
-//   final     discounted cash flows and the European control variate are
-//             reduced with the deterministic last-block finaliser.
+//   final     discounted cash flows and the martingale control variate are
+//             averaged over antithetic pairs and reduced with the
+//             deterministic last-block finaliser (cooperative launch) or
+//             through distributed shared memory (cluster launch).
 // Per-path state (cash flow, exercise date) stays in shared memory for the
 // whole sweep. The regression basis is {1, x, x^2} with x = (S - E)/E: the
 // reference's S - E rescaled, the same fitted values in exact arithmetic.
@@ -53,7 +55,8 @@ constexpr size_t kLsmMaxSmem = 227 * 1024;
 struct LsmParams {
   float pf, nK, E, invE;  // payoff = max(pf S + nK, 0); x = (S - E) * invE
   float a2, b2, l2S0;     // per-date log2 drift / vol, log2 S0
-  float gdisc;            // exp(-rT), for the control variate
+  float gdisc;            // exp(-rT)
+  float rf, sigf, dtf;    // r, sigma, T/M: the European price of the control variate
   int M, ref_exercise;
   long long H;            // antithetic pairs = N / 2
   long long Hp;           // H rounded up to a multiple of 4
@@ -75,6 +78,19 @@ struct LsmParams {
 
 __device__ __forceinline__ float lsm_payoff(const LsmParams& P, float S) {
   return fmaxf(fmaf(P.pf, S, P.nK), 0.f);
+}
+
+__device__ __forceinline__ float norm_cdf_f(float x) { return 0.5f * erfcf(-x * 0.70710678f); }
+
+// Black-Scholes price of the European option with time `rem` to expiry, FP32.
+__device__ float european_price(const LsmParams& P, float S, float rem) {
+  const float sd = P.sigf * sqrtf(rem);
+  const float dK = P.E * expf(-P.rf * rem);
+  if (!(sd > 0.f)) return fmaxf(P.pf * (S - dK), 0.f);
+  const float d1 = (logf(S * P.invE) + (P.rf + 0.5f * P.sigf * P.sigf) * rem) / sd;
+  const float d2 = d1 - sd;
+  if (P.pf > 0.f) return S * norm_cdf_f(d1) - dK * norm_cdf_f(d2);
+  return dK * norm_cdf_f(-d2) - S * norm_cdf_f(-d1);
 }
 
 // include/common.h:98-141: adjugate over the determinant, then the mat-vec
@@ -409,21 +425,43 @@ __device__ void lsm_body(const LsmParams& P, int b) {
     return;
   }
 
-  // ---- discounted cash flows and the European control variate ----
+  // ---- discounted cash flows and the control variate, per antithetic pair ----
+  // Moments are taken over pair means: the two paths of a pair share their
+  // draws, so the pair, not the path, is the independent sample.
+  // Control variate (martingale CV): g = e^{-r tau} P_E(S_tau, T - tau), the
+  // discounted European price at the path's exercise time. The discounted
+  // European price is a martingale, so E[g] = P_E(S0, T) for any stopping
+  // time. S_tau is E + pf*cf where the path exercised (or finished in the
+  // money) and S_M from the last row otherwise.
   const float* last = P.paths + (size_t)(M - 1) * 2 * P.Hp;
   KSum sy, syy, sg, sgg, syg;
   for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+    float y2 = 0.f, g2 = 0.f;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int s = h * PB + i;
-      const float y = S.cf[s] * S.dt[S.tau[s]];
-      const float g = P.gdisc * lsm_payoff(P, last[h * P.Hp + p0 + i]);
-      sy.add(y);
-      syy.add(y * y);
-      sg.add(g);
-      sgg.add(g * g);
-      syg.add(y * g);
+      const int tau = S.tau[s];
+      const float cf = S.cf[s];
+      y2 += cf * S.dt[tau];
+      float g;
+      if (P.ref_exercise) {
+        // The reference's exercise value does not identify S_tau: use the
+        // discounted European payoff at T (mean: the same P_E(S0, T)).
+        g = S.dt[M] * lsm_payoff(P, last[h * P.Hp + p0 + i]);
+      } else if (tau == M) {
+        g = cf * S.dt[M];  // European payoff at T (cf is payoff(S_M)), discounted
+      } else {
+        const float St = P.E + P.pf * cf;
+        g = S.dt[tau] * european_price(P, St, (float)(M - tau) * P.dtf);
+      }
+      g2 += g;
     }
+    const float y = 0.5f * y2, g = 0.5f * g2;
+    sy.add(y);
+    syy.add(y * y);
+    sg.add(g);
+    sgg.add(g * g);
+    syg.add(y * g);
   }
   DF v[kMoments] = {df_of(sy), df_of(syy), df_of(sg), df_of(sgg), df_of(syg)};
   DF tot[kMoments];
@@ -483,6 +521,9 @@ void lsm_fill(LsmParams& P, double S0, double E, double r, double sigma, double 
   P.b2 = (float)(sigma * sqrt(dtd) * log2e);
   P.l2S0 = (float)(log(S0) * log2e);
   P.gdisc = (float)exp(-r * T);
+  P.rf = (float)r;
+  P.sigf = (float)sigma;
+  P.dtf = (float)dtd;
   P.M = M;
   P.ref_exercise = ref_exercise ? 1 : 0;
   P.H = N / 2;
@@ -527,7 +568,9 @@ int check_lsm_request(double S0, double E, double r, double sigma, double T, lon
 
 void fill_amer_result(const double* s, long long N, double S0, double E, double r, double sigma,
                       double T, int pf, bool use_cv, pcf_mc_result* out) {
-  fill_result(s, N, bs_price(S0, E, r, sigma, T, pf), 1.0, use_cv, out);
+  // The sums run over N/2 antithetic pair means (the independent samples).
+  fill_result(s, N / 2, bs_price(S0, E, r, sigma, T, pf), 1.0, use_cv, out);
+  out->n_paths = N;
   // src/mc_amer.cpp:113: the price is at least the immediate exercise value.
   const double intrinsic = std::max(pf * (S0 - E), 0.0);
   out->price = std::max(out->price, intrinsic);
@@ -581,115 +624,162 @@ int lsm_cluster_size(pcf_ctx* c) {
   return cached;
 }
 
-int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmBatch** out) {
-  *out = nullptr;
-  LsmBatch* B = new LsmBatch();
-  const int CL = lsm_cluster_size(c);
-  const int kPB[] = {512, 1024, 2048, 4096, 8192};
-  // Assign shapes.
-  std::vector<int> cls(reqs.size(), -1);  // index into kPB, or -1 for cooperative
-  for (size_t i = 0; i < reqs.size(); ++i) {
+// Shapes and device layout of a batch: params tables | discount tables (the
+// uploaded prefix) | cooperative scratch | path matrices.
+struct LsmLayout {
+  int CL = 8;
+  std::vector<int> cls;  // index into kLsmPB, or -1 for the cooperative kernel
+  std::vector<std::vector<int>> members;
+  std::vector<size_t> o_params, o_dt, o_paths, o_coop;
+  std::vector<int> coop_G, coop_PB;
+  std::vector<size_t> coop_sm;
+  size_t upload = 0, total = 0;
+};
+
+constexpr int kLsmPB[] = {512, 1024, 2048, 4096, 8192};
+
+int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
+  const size_t n = reqs.size();
+  L.CL = lsm_cluster_size(c);
+  L.cls.assign(n, -1);
+  for (size_t i = 0; i < n; ++i) {
     const long long H = reqs[i].N / 2;
     for (int k = 0; k < 5; ++k)
-      if ((long long)CL * kPB[k] >= H &&
-          lsm_smem(kPB[k], reqs[i].M) + kStaticSmemReserve <= kLsmMaxSmem) {
-        cls[i] = k;
+      if ((long long)L.CL * kLsmPB[k] >= H &&
+          lsm_smem(kLsmPB[k], reqs[i].M) + kStaticSmemReserve <= kLsmMaxSmem) {
+        L.cls[i] = k;
         break;
       }
   }
-  // Device layout: params tables | dtabs | path matrices | coop scratch.
-  std::vector<LsmParams> host;
-  std::vector<std::vector<int>> members(5);
-  for (size_t i = 0; i < reqs.size(); ++i)
-    if (cls[i] >= 0) members[cls[i]].push_back((int)i);
+  L.members.assign(5, {});
+  for (size_t i = 0; i < n; ++i)
+    if (L.cls[i] >= 0) L.members[L.cls[i]].push_back((int)i);
   size_t off = 0;
-  std::vector<size_t> o_params(5, 0);
+  L.o_params.assign(5, 0);
   for (int k = 0; k < 5; ++k) {
-    o_params[k] = off;
-    off = a256(off + sizeof(LsmParams) * members[k].size());
+    L.o_params[k] = off;
+    off = a256(off + sizeof(LsmParams) * L.members[k].size());
   }
-  std::vector<size_t> o_dt(reqs.size()), o_paths(reqs.size()), o_coop(reqs.size(), 0);
-  for (size_t i = 0; i < reqs.size(); ++i) {
-    o_dt[i] = off;
+  L.o_dt.assign(n, 0);
+  for (size_t i = 0; i < n; ++i) {
+    L.o_dt[i] = off;
     off = a256(off + sizeof(float) * (reqs[i].M + 1));
   }
-  for (size_t i = 0; i < reqs.size(); ++i) {
-    o_paths[i] = off;
+  L.upload = off;
+  L.coop_G.assign(n, 0);
+  L.coop_PB.assign(n, 0);
+  L.coop_sm.assign(n, 0);
+  L.o_coop.assign(n, 0);
+  for (size_t i = 0; i < n; ++i) {
+    if (L.cls[i] >= 0) continue;
+    if (!coop_shape(c, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i], L.coop_sm[i]))
+      return set_error(PCF_EINVAL, "American request with N = %lld is too large", reqs[i].N);
+    L.o_coop[i] = off;  // partial (2 G 8 float2) | fpartial (G 5 float2) | 2 counters
+    off = a256(off + 8 * (2 * (size_t)L.coop_G[i] * kRegSums + (size_t)L.coop_G[i] * kMoments) +
+               16);
+  }
+  L.o_paths.assign(n, 0);
+  for (size_t i = 0; i < n; ++i) {
+    L.o_paths[i] = off;
     const long long Hp = ((reqs[i].N / 2) + 3) & ~3LL;
     off = a256(off + sizeof(float) * (size_t)reqs[i].M * 2 * (size_t)Hp);
   }
-  std::vector<int> coop_G(reqs.size(), 0), coop_PB(reqs.size(), 0);
-  std::vector<size_t> coop_sm(reqs.size(), 0);
-  for (size_t i = 0; i < reqs.size(); ++i) {
-    if (cls[i] >= 0) continue;
-    if (!coop_shape(c, reqs[i].N / 2, reqs[i].M, coop_G[i], coop_PB[i], coop_sm[i])) {
+  L.total = std::max(off, (size_t)256);
+  return PCF_OK;
+}
+
+int lsm_batch_bytes(pcf_ctx* c, const std::vector<LsmRequest>& reqs, size_t* dev,
+                    size_t* host) {
+  LsmLayout L;
+  const int st = lsm_layout(c, reqs, L);
+  if (st) return st;
+  *dev = L.total;
+  *host = L.upload;
+  return PCF_OK;
+}
+
+int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream_t s,
+                     ExtMem* mem, LsmBatch** out) {
+  *out = nullptr;
+  LsmLayout Lo;
+  int st = lsm_layout(c, reqs, Lo);
+  if (st) return st;
+  LsmBatch* B = new LsmBatch();
+  char* d = nullptr;
+  char* h = nullptr;
+  std::vector<char> hown;
+  if (mem) {
+    d = mem->dalloc(Lo.total);
+    h = mem->halloc(Lo.upload);
+    if (!d || !h) {
       delete B;
-      return set_error(PCF_EINVAL, "American request with N = %lld is too large", reqs[i].N);
+      return set_error(PCF_ENOMEM, "American batch needs %zu device bytes; the slot is full",
+                       Lo.total);
     }
-    o_coop[i] = off;  // partial (2 G 8 float2) | fpartial (G 5 float2) | 2 counters
-    off = a256(off + 8 * (2 * (size_t)coop_G[i] * kRegSums + (size_t)coop_G[i] * kMoments) + 16);
+  } else {
+    if (c->budget_bytes && Lo.total > c->budget_bytes) {
+      delete B;
+      return set_error(PCF_ENOMEM, "American batch needs %zu device bytes, over the budget",
+                       Lo.total);
+    }
+    st = cuda_status(cudaMalloc(&B->d_mem, Lo.total), "cudaMalloc(LSM batch)");
+    if (st) {
+      delete B;
+      return st;
+    }
+    d = (char*)B->d_mem;
+    hown.assign(Lo.upload, 0);
+    h = hown.data();
   }
-  if (c->budget_bytes && off > c->budget_bytes) {
-    delete B;
-    return set_error(PCF_ENOMEM, "American batch needs %zu device bytes, over the budget", off);
-  }
-  int st = cuda_status(cudaMalloc(&B->d_mem, std::max(off, (size_t)256)), "cudaMalloc(LSM batch)");
-  if (st) {
-    delete B;
-    return st;
-  }
-  B->bytes = off;
-  char* d = (char*)B->d_mem;
-  std::vector<char> h(off, 0);
+  B->bytes = Lo.total;
   auto fill = [&](size_t i, LsmParams& P) {
     const LsmRequest& q = reqs[i];
     lsm_fill(P, q.S0, q.E, q.r, q.sigma, q.T, q.N, q.M, q.pf, q.ref_exercise, q.seed, q.stream);
-    dtab_fill((float*)&h[o_dt[i]], q.r, q.T, q.M);
-    P.dtab = (const float*)(d + o_dt[i]);
-    P.paths = (float*)(d + o_paths[i]);
+    dtab_fill((float*)(h + Lo.o_dt[i]), q.r, q.T, q.M);
+    P.dtab = (const float*)(d + Lo.o_dt[i]);
+    P.paths = (float*)(d + Lo.o_paths[i]);
     P.out = q.d_out;
     P.err = q.d_flags;
     P.singular = q.d_flags + 1;
   };
   for (int k = 0; k < 5; ++k) {
-    if (members[k].empty()) continue;
+    if (Lo.members[k].empty()) continue;
     LsmCluster L;
-    L.CL = CL;
-    L.PB = kPB[k];
-    L.C = (int)members[k].size();
+    L.CL = Lo.CL;
+    L.PB = kLsmPB[k];
+    L.C = (int)Lo.members[k].size();
     int Mmax = 2;
-    LsmParams* tab = (LsmParams*)&h[o_params[k]];
+    LsmParams* tab = (LsmParams*)(h + Lo.o_params[k]);
     for (int j = 0; j < L.C; ++j) {
-      const int i = members[k][j];
+      const int i = Lo.members[k][j];
       fill(i, tab[j]);
       tab[j].pairs_per_block = L.PB;
-      tab[j].nblocks = CL;
+      tab[j].nblocks = Lo.CL;
       Mmax = std::max(Mmax, reqs[i].M);
     }
     L.smem = lsm_smem(L.PB, Mmax);
-    L.d_params = (LsmParams*)(d + o_params[k]);
+    L.d_params = (LsmParams*)(d + Lo.o_params[k]);
     B->clusters.push_back(L);
   }
   for (size_t i = 0; i < reqs.size(); ++i) {
-    if (cls[i] >= 0) continue;
+    if (Lo.cls[i] >= 0) continue;
     LsmParams P;
     fill(i, P);
-    P.pairs_per_block = coop_PB[i];
-    P.nblocks = coop_G[i];
-    char* base = d + o_coop[i];
+    P.pairs_per_block = Lo.coop_PB[i];
+    P.nblocks = Lo.coop_G[i];
+    char* base = d + Lo.o_coop[i];
     P.partial = (double*)base;
-    P.fpartial = (double*)(base + 8 * 2 * (size_t)coop_G[i] * kRegSums);
-    unsigned* cnt = (unsigned*)(base + 8 * (2 * (size_t)coop_G[i] * kRegSums +
-                                            (size_t)coop_G[i] * kMoments));
+    P.fpartial = (double*)(base + 8 * 2 * (size_t)Lo.coop_G[i] * kRegSums);
+    unsigned* cnt = (unsigned*)(base + 8 * (2 * (size_t)Lo.coop_G[i] * kRegSums +
+                                            (size_t)Lo.coop_G[i] * kMoments));
     P.barrier = cnt;
     P.ticket = cnt + 1;
     B->coop.push_back(P);
-    B->coop_grid.push_back(coop_G[i]);
-    B->coop_smem.push_back(coop_sm[i]);
+    B->coop_grid.push_back(Lo.coop_G[i]);
+    B->coop_smem.push_back(Lo.coop_sm[i]);
   }
-  st = cuda_status(cudaMemcpyAsync(d, h.data(), off, cudaMemcpyHostToDevice, c->stream),
-                   "H2D LSM batch");
-  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "LSM batch upload");
+  st = cuda_status(cudaMemcpyAsync(d, h, Lo.upload, cudaMemcpyHostToDevice, s), "H2D LSM batch");
+  if (!st && !mem) st = cuda_status(cudaStreamSynchronize(s), "LSM batch upload");
   if (st) {
     lsm_batch_destroy(B);
     return st;

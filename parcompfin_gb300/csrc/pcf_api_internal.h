@@ -68,7 +68,32 @@ int check_lsm_request(double S0, double E, double r, double sigma, double T, lon
                       int pf);
 void fill_amer_result(const double* s, long long N, double S0, double E, double r, double sigma,
                       double T, int pf, bool use_cv, pcf_mc_result* out);
-int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmBatch** out);
+// Caller-provided memory for building a batch without allocating: bump
+// allocation from a device region and a pinned host region (256-byte aligned).
+struct ExtMem {
+  char* d = nullptr;
+  size_t d_cap = 0, d_used = 0;
+  char* h = nullptr;
+  size_t h_cap = 0, h_used = 0;
+  char* dalloc(size_t n) {
+    const size_t o = (d_used + 255) & ~(size_t)255;
+    if (o + n > d_cap) return nullptr;
+    d_used = o + n;
+    return d + o;
+  }
+  char* halloc(size_t n) {
+    const size_t o = (h_used + 255) & ~(size_t)255;
+    if (o + n > h_cap) return nullptr;
+    h_used = o + n;
+    return h + o;
+  }
+};
+int lsm_batch_bytes(pcf_ctx* c, const std::vector<LsmRequest>& reqs, size_t* dev,
+                    size_t* host);
+// With mem == NULL the batch allocates its own device memory and uploads
+// synchronously; otherwise it takes memory from mem and only queues the upload on s.
+int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream_t s,
+                     ExtMem* mem, LsmBatch** out);
 int lsm_batch_launch(pcf_ctx* c, LsmBatch* b, cudaStream_t s);
 int lsm_batch_kernels(const LsmBatch* b);
 void lsm_batch_destroy(LsmBatch* b);

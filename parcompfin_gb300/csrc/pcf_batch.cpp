@@ -2,9 +2,17 @@
 //
 // A plan groups requests by method and uploads, once, each group's contract
 // table, the item prefix table and the basket factors. A launch is then one
-// memset (the groups' completion tickets and work-queue heads) plus one
-// persistent kernel per method group, with no host traffic, so a plan can be
-// replayed or captured in a CUDA graph. Results are read back in one copy.
+// memset plus one persistent kernel per Monte Carlo method group, and the
+// American contracts' launches. The memset clears the groups' completion
+// tickets, the work-queue heads and the American flag words. No host traffic
+// happens at launch, so a plan can be replayed or captured in a CUDA graph.
+// Results are read back in one copy.
+//
+// plan_build() either owns its memory (the public API: cudaMalloc, synchronous
+// upload) or builds inside caller-provided memory without allocating and only
+// queues the upload (the serving loop, which reserves its memory up front).
+#include "pcf_plan_internal.h"
+
 #include <math.h>
 #include <string.h>
 
@@ -12,53 +20,16 @@
 #include <numeric>
 #include <vector>
 
-#include "pcf_api_internal.h"
 #include "pcf_math.h"
 
 using namespace pcf;
 
 namespace {
 
-struct Group {
-  McMethod method;
-  int max_d = 0;
-  std::vector<int> req;           // request index of each contract (queue order)
-  std::vector<McContract> cs;
-  std::vector<float> fb;
-  std::vector<int> start;         // item prefix, size C+1
-  McLaunch L{};
-  int grid = 0;
-};
-
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-}  // namespace
-
-struct pcf_plan {
-  pcf_ctx* ctx = nullptr;
-  int n = 0;
-  std::vector<Group> groups;
-  std::vector<long long> npaths;
-  std::vector<double> mu_g, disc;
-  std::vector<int> use_cv;
-  std::vector<int> out_slot;  // request -> row of the device out table
-  void* d_mem = nullptr;
-  double* h_out = nullptr;
-  unsigned* d_tickets = nullptr;
-  size_t tickets_bytes = 0;
-  double* d_out = nullptr;
-  // American requests: priced by an LSM batch; two flag words each (wait gave
-  // up, singular dates) live in the ticket region, so the per-launch memset
-  // clears them.
-  LsmBatch* lsm = nullptr;
-  std::vector<int> amer;              // request indices
-  std::vector<pcf_mc_request> amer_q; // their parameters (for the estimators)
-  int* d_amer_flags = nullptr;
-  int* h_amer_flags = nullptr;
-};
-
-static int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContract& k,
-                         std::vector<float>& fb, double& mu_g, double& disc) {
+int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContract& k,
+                  std::vector<float>& fb, double& mu_g, double& disc) {
   int st = check_common(q.method == PCF_METHOD_BASKET && q.basket_S0 ? 1.0 : q.S0, q.E, q.r,
                         q.sigma, q.T, q.N, q.payoff_fun);
   if (st) return set_error(st, "request %d: %s", idx, pcf_last_error());
@@ -104,26 +75,33 @@ static int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContrac
   }
 }
 
-extern "C" {
+// Basket launches are split by width class so narrow baskets do not run in
+// the register-heavy instantiation of wide ones.
+int basket_class(int d) { return d <= 4 ? 0 : d <= 8 ? 1 : d <= 16 ? 2 : d <= 32 ? 3 : 4; }
 
-int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** out) {
-  if (!out || (n > 0 && !reqs) || n < 0) return set_error(PCF_EINVAL, "bad plan arguments");
+}  // namespace
+
+namespace pcf {
+
+int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, ExtMem* mem,
+               pcf_plan** out) {
   *out = nullptr;
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
   pcf_plan* p = new pcf_plan();
   p->ctx = c;
+  p->stream = s;
   p->n = n;
   p->npaths.resize(n);
   p->mu_g.resize(n);
   p->disc.resize(n);
   p->use_cv.resize(n);
   p->out_slot.resize(n);
-  Group g[3];
+  // Groups: European, Asian, then one per basket width class.
+  const int kGroups = 7;
+  std::vector<Group> g(kGroups);
   g[0].method = MC_EUR;
   g[1].method = MC_ASIA;
-  g[2].method = MC_BASKET;
+  for (int k = 2; k < kGroups; ++k) g[k].method = MC_BASKET;
+  int st;
   for (int i = 0; i < n; ++i) {
     const int m = reqs[i].method;
     if (m == PCF_METHOD_AMER) {
@@ -143,17 +121,18 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
       delete p;
       return set_error(PCF_EINVAL, "request %d: method %d not supported in a batch", i, m);
     }
+    const int gi = m == PCF_METHOD_BASKET ? 2 + basket_class(reqs[i].assets) : m;
     McContract k;
-    st = build_request(c, reqs[i], i, k, g[m].fb, p->mu_g[i], p->disc[i]);
+    st = build_request(c, reqs[i], i, k, g[gi].fb, p->mu_g[i], p->disc[i]);
     if (st) {
       delete p;
       return st;
     }
-    if (m == PCF_METHOD_BASKET) g[m].max_d = std::max(g[m].max_d, reqs[i].assets);
+    if (m == PCF_METHOD_BASKET) g[gi].max_d = std::max(g[gi].max_d, reqs[i].assets);
     p->npaths[i] = reqs[i].N;
     p->use_cv[i] = reqs[i].use_cv != 0;
-    g[m].cs.push_back(k);
-    g[m].req.push_back(i);
+    g[gi].cs.push_back(k);
+    g[gi].req.push_back(i);
   }
   // Longest items first: the queue then ends on short items (load balance).
   for (Group& gr : g) {
@@ -171,8 +150,9 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
     gr.req.swap(req2);
     if (!gr.cs.empty()) p->groups.push_back(gr);
   }
-  // Device layout: per group [contracts | item_start | factors | partials],
-  // then all tickets+queues, then the out table (n x kMoments).
+  // Device layout: per group [contracts | item_start | factors] (the uploaded
+  // prefix), then per group [partials], the tickets (+ queues, + American
+  // flags) and the out table (n x kMoments).
   size_t off = 0;
   std::vector<size_t> o_con, o_start, o_fb, o_part, o_tick;
   size_t ticket_words = 0;
@@ -192,10 +172,13 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
     off = a256(off + sizeof(int) * (C + 1));
     o_fb.push_back(off);
     off = a256(off + sizeof(float) * gr.fb.size());
+  }
+  const size_t upload = off;
+  for (Group& gr : p->groups) {
     o_part.push_back(off);
-    off = a256(off + sizeof(double) * kMoments * (size_t)gr.start[C]);
+    off = a256(off + sizeof(double) * kMoments * (size_t)gr.start[gr.cs.size()]);
     o_tick.push_back(ticket_words);
-    ticket_words += (size_t)C + 1;
+    ticket_words += gr.cs.size() + 1;
   }
   const size_t o_tickets = off;
   const size_t amer_flag_word = ticket_words;
@@ -204,31 +187,44 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
   off = a256(off + p->tickets_bytes);
   const size_t o_out = off;
   off = a256(off + sizeof(double) * kMoments * (size_t)std::max(n, 1));
-  if (c->budget_bytes && off > c->budget_bytes) {
-    delete p;
-    return set_error(PCF_ENOMEM, "plan needs %zu device bytes, over the context budget", off);
+  const size_t host_out = sizeof(double) * kMoments * std::max(n, 1) +
+                          sizeof(int) * 2 * (p->amer.size() + 1);
+  char* d = nullptr;
+  char* hup = nullptr;
+  std::vector<char> hown;
+  if (mem) {
+    d = mem->dalloc(off);
+    hup = mem->halloc(std::max(upload, (size_t)1));
+    p->h_out = (double*)mem->halloc(host_out);
+    if (!d || !hup || !p->h_out) {
+      delete p;
+      return set_error(PCF_ENOMEM, "batch needs %zu device bytes; the slot is full", off);
+    }
+  } else {
+    if (c->budget_bytes && off > c->budget_bytes) {
+      delete p;
+      return set_error(PCF_ENOMEM, "plan needs %zu device bytes, over the context budget", off);
+    }
+    st = cuda_status(cudaMalloc(&p->d_mem, off), "cudaMalloc(plan)");
+    if (!st) st = cuda_status(cudaMallocHost(&p->h_own, host_out), "cudaMallocHost(plan)");
+    if (st) {
+      pcf_plan_destroy(p);
+      return st;
+    }
+    p->h_out = (double*)p->h_own;
+    d = (char*)p->d_mem;
+    hown.assign(std::max(upload, (size_t)1), 0);
+    hup = hown.data();
   }
-  st = cuda_status(cudaMalloc(&p->d_mem, off), "cudaMalloc(plan)");
-  if (!st) st = cuda_status(cudaMallocHost((void**)&p->h_out,
-                                           sizeof(double) * kMoments * std::max(n, 1) +
-                                               sizeof(int) * 2 * (p->amer.size() + 1)),
-                            "cudaMallocHost(plan)");
-  if (st) {
-    pcf_plan_destroy(p);
-    return st;
-  }
-  char* d = (char*)p->d_mem;
   p->d_tickets = (unsigned*)(d + o_tickets);
   p->d_out = (double*)(d + o_out);
-  // Upload every table with one staging buffer.
-  std::vector<char> host(o_tickets, 0);
   int row = 0;
   for (size_t gi = 0; gi < p->groups.size(); ++gi) {
     Group& gr = p->groups[gi];
     const int C = (int)gr.cs.size();
-    memcpy(&host[o_con[gi]], gr.cs.data(), sizeof(McContract) * C);
-    memcpy(&host[o_start[gi]], gr.start.data(), sizeof(int) * (C + 1));
-    if (!gr.fb.empty()) memcpy(&host[o_fb[gi]], gr.fb.data(), sizeof(float) * gr.fb.size());
+    memcpy(hup + o_con[gi], gr.cs.data(), sizeof(McContract) * C);
+    memcpy(hup + o_start[gi], gr.start.data(), sizeof(int) * (C + 1));
+    if (!gr.fb.empty()) memcpy(hup + o_fb[gi], gr.fb.data(), sizeof(float) * gr.fb.size());
     for (int i = 0; i < C; ++i) p->out_slot[gr.req[i]] = row + i;
     McLaunch& L = gr.L;
     L.contracts = (const McContract*)(d + o_con[gi]);
@@ -246,11 +242,10 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
     gr.grid = std::min(L.total_items, c->sm_count * mc_max_active_blocks(gr.method, gr.max_d));
     row += C;
   }
-  if (o_tickets) {
-    st = cuda_status(cudaMemcpyAsync(d, host.data(), o_tickets, cudaMemcpyHostToDevice,
-                                     c->stream),
+  if (upload) {
+    st = cuda_status(cudaMemcpyAsync(d, hup, upload, cudaMemcpyHostToDevice, s),
                      "H2D plan tables");
-    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "plan upload");
+    if (!st && !mem) st = cuda_status(cudaStreamSynchronize(s), "plan upload");
     if (st) {
       pcf_plan_destroy(p);
       return st;
@@ -279,7 +274,7 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
       p->out_slot[p->amer[a]] = row++;
       lr.push_back(x);
     }
-    st = lsm_batch_create(c, lr, &p->lsm);
+    st = lsm_batch_create(c, lr, s, mem, &p->lsm);
     if (st) {
       pcf_plan_destroy(p);
       return st;
@@ -289,44 +284,37 @@ int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** 
   return PCF_OK;
 }
 
-int pcf_plan_launch(pcf_plan* p) {
-  if (!p) return set_error(PCF_EINVAL, "plan is NULL");
+int plan_launch(pcf_plan* p) {
   pcf_ctx* c = p->ctx;
-  cudaSetDevice(c->device);
   if (p->tickets_bytes) {
-    int st = cuda_status(cudaMemsetAsync(p->d_tickets, 0, p->tickets_bytes, c->stream),
+    int st = cuda_status(cudaMemsetAsync(p->d_tickets, 0, p->tickets_bytes, p->stream),
                          "memset tickets");
     if (st) return st;
   }
   for (Group& gr : p->groups) {
-    int st = cuda_status(launch_mc(gr.method, gr.L, gr.grid, gr.max_d, c->stream),
+    int st = cuda_status(launch_mc(gr.method, gr.L, gr.grid, gr.max_d, p->stream),
                          "batch kernel launch");
     if (st) return st;
     c->launches += 1;
   }
-  if (p->lsm) return lsm_batch_launch(c, p->lsm, c->stream);
+  if (p->lsm) return lsm_batch_launch(c, p->lsm, p->stream);
   return PCF_OK;
 }
 
-int pcf_plan_kernel_count(const pcf_plan* p) {
-  return p ? (int)p->groups.size() + (p->lsm ? lsm_batch_kernels(p->lsm) : 0) : 0;
-}
-
-int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
-  if (!p || (p->n && !results)) return set_error(PCF_EINVAL, "bad arguments");
-  pcf_ctx* c = p->ctx;
-  cudaSetDevice(c->device);
+int plan_fetch(pcf_plan* p) {
   if (p->n == 0) return PCF_OK;
   int st = cuda_status(cudaMemcpyAsync(p->h_out, p->d_out, sizeof(double) * kMoments * p->n,
-                                       cudaMemcpyDeviceToHost, c->stream),
+                                       cudaMemcpyDeviceToHost, p->stream),
                        "D2H batch results");
   if (!st && !p->amer.empty())
     st = cuda_status(cudaMemcpyAsync(p->h_amer_flags, p->d_amer_flags,
                                      sizeof(int) * 2 * p->amer.size(), cudaMemcpyDeviceToHost,
-                                     c->stream),
+                                     p->stream),
                      "D2H American flags");
-  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "batch kernels");
-  if (st) return st;
+  return st;
+}
+
+int plan_fill_results(pcf_plan* p, pcf_mc_result* results) {
   for (int i = 0; i < p->n; ++i)
     fill_result(p->h_out + (size_t)p->out_slot[i] * kMoments, p->npaths[i], p->mu_g[i],
                 p->disc[i], p->use_cv[i] != 0, &results[i]);
@@ -341,21 +329,52 @@ int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
       // A request whose sweep failed gets NaN; the call reports the first failure.
       results[i].price = results[i].price_plain = results[i].price_cv = NAN;
       if (status == PCF_OK)
-        status = set_error(fl[0] ? PCF_ETIMEOUT : PCF_ESINGULAR,
-                           "request %d: %s", i, fl[0] ? "LSM device wait gave up"
-                                                      : "Detereminant is not > 0");
+        status = set_error(fl[0] ? PCF_ETIMEOUT : PCF_ESINGULAR, "request %d: %s", i,
+                           fl[0] ? "LSM device wait gave up" : "Detereminant is not > 0");
     }
   }
   return status;
 }
 
+}  // namespace pcf
+
+extern "C" {
+
+int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** out) {
+  if (!out || (n > 0 && !reqs) || n < 0) return set_error(PCF_EINVAL, "bad plan arguments");
+  *out = nullptr;
+  int st;
+  pcf_ctx* c = resolve_ctx(ctx, &st);
+  if (!c) return st;
+  return plan_build(c, n, reqs, c->stream, nullptr, out);
+}
+
+int pcf_plan_launch(pcf_plan* p) {
+  if (!p) return set_error(PCF_EINVAL, "plan is NULL");
+  cudaSetDevice(p->ctx->device);
+  return plan_launch(p);
+}
+
+int pcf_plan_kernel_count(const pcf_plan* p) {
+  return p ? (int)p->groups.size() + (p->lsm ? lsm_batch_kernels(p->lsm) : 0) : 0;
+}
+
+int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
+  if (!p || (p->n && !results)) return set_error(PCF_EINVAL, "bad arguments");
+  cudaSetDevice(p->ctx->device);
+  int st = plan_fetch(p);
+  if (!st) st = cuda_status(cudaStreamSynchronize(p->stream), "batch kernels");
+  if (st) return st;
+  return plan_fill_results(p, results);
+}
+
 int pcf_plan_destroy(pcf_plan* p) {
   if (!p) return PCF_OK;
   cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
+  cudaStreamSynchronize(p->stream);
   lsm_batch_destroy(p->lsm);
   if (p->d_mem) cudaFree(p->d_mem);
-  if (p->h_out) cudaFreeHost(p->h_out);
+  if (p->h_own) cudaFreeHost(p->h_own);
   delete p;
   return PCF_OK;
 }

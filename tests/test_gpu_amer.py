@@ -1,10 +1,9 @@
 """GPU parity of the Longstaff-Schwartz kernel (the reference's mc_amer).
 
 Bars:
-  * FP64 twin on identical Philox draws: the European control-variate sums
-    (no exercise decisions involved) within 1e-5 relative; the LSM price
-    within 3e-4 relative for puts and 1e-3 for calls (FP32 paths can flip
-    the exercise decision of the paths whose continuation estimate lies
+  * FP64 twin on identical Philox draws: the LSM price and the control
+    variate within 3e-4 relative for puts and 1e-3 for calls (FP32 paths can
+    flip the exercise decision of the paths whose continuation estimate lies
     within FP32 rounding of the exercise value; each flip moves the price by
     at most payoff/N);
   * puts against the reference's own lattice oracle binom_vanilla_amer
@@ -33,13 +32,14 @@ def test_amer_matches_fp64_twin(orc, ctx, pf, N, M):
     res = mc_amer_result(100, 100, .05, .3, 1.0, N, M, pf, seed=5, ctx=ctx)
     s = twin(orc, 100, 100, .05, .3, 1.0, N, M, pf, 0, 5)
     assert s[5] == 0
-    for k in (2, 3):  # European control-variate sums: decisions play no part
-        assert abs(res.sums[k] - s[k]) <= 1e-5 * abs(s[k]), (k, res.sums[k], s[k])
     # Calls on a non-dividend stock sit on the exercise boundary for many deep
     # in-the-money paths (early exercise is never optimal, the fit is only
     # just above the exercise value), so more decisions can flip: 1e-3.
+    # The control variate is evaluated at each path's exercise date, so its
+    # sums carry the same flips.
     tol = 3e-4 if pf == -1 else 1e-3
-    assert abs(res.sums[0] - s[0]) <= tol * abs(s[0]), (res.sums[0], s[0])
+    for k in (0, 2):
+        assert abs(res.sums[k] - s[k]) <= tol * abs(s[k]), (k, res.sums[k], s[k])
 
 
 def test_amer_put_against_lattice(orc, ctx):
@@ -86,7 +86,7 @@ def test_amer_call_is_a_lower_bound(orc, ctx):
     assert res.price_plain <= bs + 3 * res.std_error_plain
     assert res.price_plain > bs - 0.35
     s = twin(orc, 100, 100, .05, .3, 1.0, N, 50, 1, 0, 4)
-    assert abs(res.price_plain - s[0] / N) < 1e-3 * bs
+    assert abs(res.price_plain - s[0] / (N // 2)) < 1e-3 * bs  # sums over N/2 pair means
 
 
 def test_amer_reference_call(orc, ctx):

@@ -1,0 +1,86 @@
+"""The continuous-batching serving loop (pcf_serve_trace).
+
+  * every request of a timed mixed trace completes, at (about) its target
+    relative standard error, unless its path count hit the cap;
+  * each served result is the same as pricing that request alone at the same
+    path count (the stated tolerance is exact equality of the moment sums:
+    a request's work items and their reduction do not depend on what else is
+    in its batch);
+  * requests arriving while other batches run are admitted into other slots
+    (more than one batch in flight).
+"""
+import math
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TARGET = 5e-4
+
+
+def _trace(pcf, n, rate, seed):
+    from parcompfin_gb300 import workloads
+    spec = workloads.config4(n, seed=seed)
+    reqs = []
+    for s in spec:
+        kw = dict(use_cv=True, seed=99, stream=s["id"])
+        if s["kind"] == "eur":
+            reqs.append(pcf.request("eur", s["S0"], s["E"], s["r"], s["sigma"], s["T"], 4, "call", **kw))
+        elif s["kind"] == "asia":
+            reqs.append(pcf.request("asia", s["S0"], s["E"], s["r"], s["sigma"], s["T"], 4, "call",
+                                    M=s["M"], **kw))
+        elif s["kind"] == "basket":
+            reqs.append(pcf.request("basket", s["S0"], s["E"], s["r"], s["sigma"], s["T"], 4, "call",
+                                    assets=s["assets"], rho=s["rho"],
+                                    basket_sigma=s["basket_sigma"], **kw))
+        else:
+            reqs.append(pcf.request("amer", s["S0"], s["E"], s["r"], s["sigma"], s["T"], 2, "put",
+                                    M=s["M"], **kw))
+    return reqs, workloads.poisson_arrivals(n, rate, seed=seed + 1)
+
+
+def test_served_trace_meets_target_and_matches_alone(ctx):
+    import parcompfin_gb300 as pcf
+    reqs, arr = _trace(pcf, 240, 4000.0, 3)
+    out, st = pcf.serve_trace(reqs, arr, target_rel_se=TARGET, ctx=ctx)
+    assert st.completed == len(reqs)
+    assert st.p50_ms <= st.p99_ms <= st.max_ms
+    assert st.batches >= 2
+    rels = []
+    for q, o in zip(reqs, out):
+        assert o.status == 0
+        r = o.result
+        assert o.done_s >= o.admit_s >= o.arrival_s - 1e-9
+        main_n = r.n_paths
+        capped = q["method"] == 3 and main_n >= (1 << 21)
+        rel = r.std_error / abs(r.price)
+        rels.append(rel)
+        if not capped:
+            # the pilot's variance estimate is itself noisy: allow 35 %
+            assert rel < 1.35 * TARGET, (q, rel)
+    # Same alone: re-price a sample of requests alone at the served path count.
+    for i in range(0, len(reqs), 12):
+        q = dict(reqs[i], N=out[i].result.n_paths)
+        alone = pcf.price_batch([q], ctx=ctx)[0]
+        assert list(alone.sums) == list(out[i].result.sums), q
+    assert sorted(rels)[len(rels) // 2] < TARGET
+
+
+def test_served_european_prices_agree_with_black_scholes(orc, ctx):
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("eur", 100, E, .05, .2, 1.0, 4, "call", use_cv=True, seed=5, stream=k)
+            for k, E in enumerate((90.0, 100.0, 110.0, 120.0))]
+    out, st = pcf.serve_trace(reqs, [0.0] * 4, target_rel_se=TARGET, ctx=ctx)
+    for q, o in zip(reqs, out):
+        bs = orc.orc_bs_price(100, q["E"], .05, .2, 1.0, 1)
+        assert abs(o.result.price - bs) < 4 * o.result.std_error + 1e-9
+
+
+def test_serving_without_target_uses_request_sizes(ctx):
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("eur", 100, 100, .05, .2, 1.0, 100_000 + k, "call", seed=1, stream=k)
+            for k in range(20)]
+    out, st = pcf.serve_trace(reqs, [0.001 * k for k in range(20)], target_rel_se=0.0, ctx=ctx)
+    assert st.completed == 20
+    for q, o in zip(reqs, out):
+        assert o.result.n_paths == q["N"] and o.paths == q["N"]

@@ -159,8 +159,18 @@ def test_twin_amer_put_near_lattice(orc):
     out = (C.c_double * 6)()
     n = 100_000
     orc.twin_mc_amer(100, 100, .05, .3, 1, n, 50, -1, 0, 5, 0, out)
-    p, se = _price_se(out, n, 1.0)
+    pairs = n // 2  # the moment sums run over antithetic pair means
+    p, se = _price_se(out, pairs, 1.0)
     lat = orc.ref_binom_vanilla_amer(100, 100, .05, .3, 1, 2000, -1.0)
     # LSM is low-biased by a few cents at 50 dates; allow that plus 4 SE.
     assert abs(p - lat) < 0.05 + 4 * se, (p, lat, se)
     assert out[5] == 0
+    # The martingale control variate has the European price as its mean and
+    # cuts the variance sharply.
+    g, se_g = _price_se([out[2], out[3]], pairs, 1.0)
+    assert abs(g - orc.orc_bs_price(100, 100, .05, .3, 1, -1)) < 4 * se_g
+    ybar, gbar = out[0] / pairs, out[2] / pairs
+    vy = out[1] / pairs - ybar * ybar
+    vg = out[3] / pairs - gbar * gbar
+    cov = out[4] / pairs - ybar * gbar
+    assert vy - cov * cov / vg < 0.2 * vy
