@@ -613,8 +613,55 @@ class MixedWorkload:
                           f"(Asian, American) each: {paths} paths in {dt:.2f} s"}
 
 
+class AmerBatchWorkload:
+    """The American leg of config 4 alone: 64 puts, one cluster each."""
+    name = "amerbatch"
+    metric = "MC paths/sec (American puts, batched Longstaff-Schwartz)"
+    unit = "paths/s"
+    dominant = "lsm_cluster_kernel"
+    C, N, M = 64, 1 << 16, 50
+
+    def __init__(self, rank):
+        import random
+        import parcompfin_gb300 as pcf
+        rng = random.Random(41 + rank)
+        self.reqs = [pcf.request("amer", 100.0, rng.uniform(90, 110), 0.05, rng.uniform(0.2, 0.4),
+                                 1.0, self.N, "put", M=self.M, use_cv=True, seed=7,
+                                 stream=rank * 4096 + i) for i in range(self.C)]
+
+    setup = EurWorkload.setup
+    step = EurWorkload.step
+    e2e = EurWorkload.e2e
+
+    def finish(self, ctx):
+        r = self.plan.results()
+        return {"median_rel_se_cv": sorted(x.std_error_cv / x.price_cv for x in r)[len(r) // 2]}
+
+    def units(self):
+        return float(self.C * self.N)
+
+    def contracts(self):
+        return float(self.C)
+
+    def config(self):
+        return {"workload": "amerbatch: 64 American puts (config-4 distribution: K~U[90,110], "
+                            "sigma~U[.2,.4], r=.05, T=1, 50 dates), 2^16 paths each, one "
+                            "16-CTA cluster per contract",
+                "paths_per_step": self.units(), "contracts_per_step": self.C}
+
+    def roofline(self, ms, sms, mhz, peaks):
+        alg = 8.0 * self.C * self.N * self.M
+        ach = alg / (ms * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+    def cpu_reference(self, threads, budget_s):
+        return LsmWorkload.cpu_reference(self, threads, budget_s)
+
+
 WORKLOADS = {w.name: w for w in (MixedWorkload, EurWorkload, AsiaWorkload, BasketWorkload,
-                                  LsmWorkload, BinomWorkload)}
+                                  LsmWorkload, BinomWorkload, AmerBatchWorkload)}
 
 
 # --------------------------------------------------------------------------
@@ -777,7 +824,7 @@ def run_ours(args, wl_cls):
         ms, e2e_med = float(t[0]), float(t[1])
     units = wl.units() * ws
     value = units / (ms * 1e-3)
-    e2e_units = (wl.e2e_units() if hasattr(wl, "e2e_units") else wl.units()) * ws
+    e2e_units = (wl.e2e_units() if hasattr(wl, "e2e_units") and e2e_ms else wl.units()) * ws
     if rank != 0:
         torch.distributed.destroy_process_group()
         return

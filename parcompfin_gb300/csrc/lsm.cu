@@ -93,26 +93,27 @@ __device__ float european_price(const LsmParams& P, float S, float rem) {
   return dK * norm_cdf_f(-d2) - S * norm_cdf_f(-d1);
 }
 
-// include/common.h:98-141: adjugate over the determinant, then the mat-vec
-// product (one reciprocal instead of nine divisions).
+// include/common.h:98-141: the adjugate over the determinant, then the
+// mat-vec product. The normal matrix of the basis {1, x, x^2} is the symmetric
+// Hankel matrix [[a0,a1,a2],[a1,a2,a3],[a2,a3,a4]], so its adjugate has six
+// distinct cofactors. They are formed with FMAs, and one reciprocal replaces
+// nine divisions. In exact arithmetic this is the reference's solution; FP64
+// is slow on GB300, so the short chain matters (it runs once per date on the
+// critical path).
 __device__ bool solve3(const double* a, double* coef) {
-  const double x[3][3] = {{a[0], a[1], a[2]}, {a[1], a[2], a[3]}, {a[2], a[3], a[4]}};
-  const double y[3] = {a[5], a[6], a[7]};
-  double det = 0;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-    det += x[0][i] * (x[1][(i + 1) % 3] * x[2][(i + 2) % 3] - x[1][(i + 2) % 3] * x[2][(i + 1) % 3]);
+  const double c00 = fma(a[2], a[4], -a[3] * a[3]);
+  const double c01 = fma(a[2], a[3], -a[1] * a[4]);
+  const double c02 = fma(a[1], a[3], -a[2] * a[2]);
+  const double c11 = fma(a[0], a[4], -a[2] * a[2]);
+  const double c12 = fma(a[1], a[2], -a[0] * a[3]);
+  const double c22 = fma(a[0], a[2], -a[1] * a[1]);
+  const double det = fma(a[0], c00, fma(a[1], c01, a[2] * c02));
   if (!(det > 0)) return false;
   const double rd = 1.0 / det;
-  double inv[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      inv[j][i] = ((x[(j + 1) % 3][(i + 1) % 3] * x[(j + 2) % 3][(i + 2) % 3]) -
-                   (x[(j + 1) % 3][(i + 2) % 3] * x[(j + 2) % 3][(i + 1) % 3])) * rd;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) coef[i] = inv[i][0] * y[0] + inv[i][1] * y[1] + inv[i][2] * y[2];
+  const double y0 = a[5], y1 = a[6], y2 = a[7];
+  coef[0] = fma(c00, y0, fma(c01, y1, c02 * y2)) * rd;
+  coef[1] = fma(c01, y0, fma(c11, y1, c12 * y2)) * rd;
+  coef[2] = fma(c02, y0, fma(c12, y1, c22 * y2)) * rd;
   return true;
 }
 
@@ -627,8 +628,8 @@ int lsm_cluster_size(pcf_ctx* c) {
 // Shapes and device layout of a batch: params tables | discount tables (the
 // uploaded prefix) | cooperative scratch | path matrices.
 struct LsmLayout {
-  int CL = 8;
   std::vector<int> cls;  // index into kLsmPB, or -1 for the cooperative kernel
+  std::vector<int> cl;   // CTAs per contract (cluster size)
   std::vector<std::vector<int>> members;
   std::vector<size_t> o_params, o_dt, o_paths, o_coop;
   std::vector<int> coop_G, coop_PB;
@@ -640,23 +641,36 @@ constexpr int kLsmPB[] = {512, 1024, 2048, 4096, 8192};
 
 int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
   const size_t n = reqs.size();
-  L.CL = lsm_cluster_size(c);
+  // Shape of each contract: a cluster of the device's full size (16 CTAs
+  // where allowed), with the smallest slice class that covers the contract.
+  // Small slices keep each CTA's shared memory low, so two CTAs share an SM
+  // and more contracts are in flight; a contract too large for a cluster
+  // runs the cooperative kernel.
+  const int CLmax = lsm_cluster_size(c);
   L.cls.assign(n, -1);
+  L.cl.assign(n, 0);
   for (size_t i = 0; i < n; ++i) {
     const long long H = reqs[i].N / 2;
+    const int cl = CLmax;
     for (int k = 0; k < 5; ++k)
-      if ((long long)L.CL * kLsmPB[k] >= H &&
+      if ((long long)cl * kLsmPB[k] >= H &&
           lsm_smem(kLsmPB[k], reqs[i].M) + kStaticSmemReserve <= kLsmMaxSmem) {
         L.cls[i] = k;
+        L.cl[i] = cl;
         break;
       }
   }
-  L.members.assign(5, {});
+  // Launch groups: one per (cluster size, slice class).
+  L.members.assign(5 * 5, {});
   for (size_t i = 0; i < n; ++i)
-    if (L.cls[i] >= 0) L.members[L.cls[i]].push_back((int)i);
+    if (L.cls[i] >= 0) {
+      int lg = 0;
+      while ((1 << lg) < L.cl[i]) ++lg;
+      L.members[lg * 5 + L.cls[i]].push_back((int)i);
+    }
   size_t off = 0;
-  L.o_params.assign(5, 0);
-  for (int k = 0; k < 5; ++k) {
+  L.o_params.assign(L.members.size(), 0);
+  for (size_t k = 0; k < L.members.size(); ++k) {
     L.o_params[k] = off;
     off = a256(off + sizeof(LsmParams) * L.members[k].size());
   }
@@ -742,11 +756,11 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
     P.err = q.d_flags;
     P.singular = q.d_flags + 1;
   };
-  for (int k = 0; k < 5; ++k) {
+  for (size_t k = 0; k < Lo.members.size(); ++k) {
     if (Lo.members[k].empty()) continue;
     LsmCluster L;
-    L.CL = Lo.CL;
-    L.PB = kLsmPB[k];
+    L.CL = 1 << (k / 5);
+    L.PB = kLsmPB[k % 5];
     L.C = (int)Lo.members[k].size();
     int Mmax = 2;
     LsmParams* tab = (LsmParams*)(h + Lo.o_params[k]);
@@ -754,7 +768,7 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
       const int i = Lo.members[k][j];
       fill(i, tab[j]);
       tab[j].pairs_per_block = L.PB;
-      tab[j].nblocks = Lo.CL;
+      tab[j].nblocks = L.CL;
       Mmax = std::max(Mmax, reqs[i].M);
     }
     L.smem = lsm_smem(L.PB, Mmax);
