@@ -7,16 +7,16 @@ Prints one JSON line (rank 0). A step is one pass of the engine over one
 batch of synthetic pricing requests (--workload; parcompfin_gb300/workloads.py
 builds the request sets):
 
-  eur     config 0: European call S0=K=100 r=.05 sigma=.2 T=1 (mc_eur,
+  eur     European call S0=K=100 r=.05 sigma=.2 T=1 (mc_eur,
           src/mc_eur.cpp:5-27), 2^28 paths per step.
-  asia    config 3: 256 Asian calls, M in {12,52,252}, N log-uniform in
+  asia    Asian book: 256 Asian calls, M in {12,52,252}, N log-uniform in
           2^16..2^22 (mc_asia, src/mc_asia.cpp:5-40), one persistent launch,
           geometric control variate.
-  basket  config 2: baskets of 4, 16, 64 assets, 2^22 paths each
+  basket  basket book: baskets of 4, 16, 64 assets, 2^22 paths each
           (mc_eur_multi, src/mc_eur_multi.cpp:6-35).
   lsm     American put by Longstaff-Schwartz, N = 2^20 paths, 50 dates
           (mc_amer, src/mc_amer.cpp:5-114).
-  binom   config 1: 1024 closed-binomial contracts, N uneven in 1e3..2e5
+  binom   binomial book: 1024 closed-binomial contracts, N uneven in 1e3..2e5
           (binom_embar, src/binom_embar.cpp:5-50), reference rounding order.
 
 value         units/s with the request tables already on the device, timed with
@@ -68,7 +68,7 @@ def _sfu_roofline(sfu_per_unit, units, ms, sms, sm_mhz):
 # --------------------------------------------------------------------------
 class EurWorkload:
     name = "eur"
-    metric = "MC paths/sec (European GBM, config-0 contract)"
+    metric = "MC paths/sec (European GBM, S0=K=100, r=.05, sigma=.2, T=1 call)"
     unit = "paths/s"
     paths = 1 << 28
     dominant = "mc_kernel<0,...> (European)"
@@ -125,20 +125,20 @@ class EurWorkload:
         price = run(n)
         dt = time.perf_counter() - t0
         return {"value": n / dt, "unit": self.unit, "cores": threads, "kind": kind,
-                "sample": f"mc_eur_omp on {n} paths of the config-0 contract, price {price:.6f}, "
+                "sample": f"mc_eur_omp on {n} paths of the ATM European call, price {price:.6f}, "
                           f"{dt:.2f} s"}
 
 
 class AsiaWorkload:
     name = "asia"
-    metric = "MC paths/sec (Asian batch, config 3)"
+    metric = "MC paths/sec (Asian batch, 256 contracts)"
     unit = "paths/s"
     dominant = "mc_kernel<1,...> (Asian, persistent)"
 
     def __init__(self, rank):
         import parcompfin_gb300 as pcf
         from parcompfin_gb300 import workloads
-        self.cs = workloads.config3()
+        self.cs = workloads.asian_book()
         self.reqs = [pcf.request("asia", c["S0"], c["E"], c["r"], c["sigma"], c["T"], c["N"], "call",
                                  M=c["M"], mode=0, use_cv=True, seed=13, stream=rank * 4096 + i)
                      for i, c in enumerate(self.cs)]
@@ -160,7 +160,7 @@ class AsiaWorkload:
         return float(sum(c["N"] * c["M"] for c in self.cs))
 
     def config(self):
-        return {"workload": "asia: config 3, 256 Asian calls (seed 13), K~U[90,110], "
+        return {"workload": "asia: 256 Asian calls (seed 13), K~U[90,110], "
                             "sigma~U[.15,.4], T~U[.5,2], M in {12,52,252}, N=2^U[16,22], "
                             "geometric control variate, one persistent launch",
                 "paths_per_step": self.units(), "path_steps_per_step": self.path_steps(),
@@ -193,21 +193,21 @@ class AsiaWorkload:
         rate_steps = done_steps / dt
         value = rate_steps * self.units() / self.path_steps()
         return {"value": value, "unit": self.unit, "cores": threads, "kind": kind,
-                "sample": f"mc_asia_omp on the config-3 contracts at N/64 ({done_paths} paths, "
+                "sample": f"mc_asia_omp on the Asian book at N/64 ({done_paths} paths, "
                           f"{done_steps} path-steps, {dt:.2f} s); paths/s scaled to the batch's "
                           "step mix"}
 
 
 class BasketWorkload:
     name = "basket"
-    metric = "MC paths/sec (basket, config 2)"
+    metric = "MC paths/sec (basket, d in {4, 16, 64})"
     unit = "paths/s"
     dominant = "mc_kernel<2,64,...> (basket)"
 
     def __init__(self, rank):
         import parcompfin_gb300 as pcf
         from parcompfin_gb300 import workloads
-        self.cs = workloads.config2()
+        self.cs = workloads.basket_book()
         self.reqs = [pcf.request("basket", 100.0, c["E"], c["r"], 0.2, c["T"], c["N"], "call",
                                  assets=c["assets"], basket_S0=c["basket_S0"],
                                  basket_sigma=c["basket_sigma"], corr=c["corr"], use_cv=True,
@@ -227,7 +227,7 @@ class BasketWorkload:
         return float(sum(c["N"] for c in self.cs))
 
     def config(self):
-        return {"workload": "basket: config 2, d in {4,16,64}, S0=K=100, r=.03, T=1, "
+        return {"workload": "basket: d in {4,16,64}, S0=K=100, r=.03, T=1, "
                             "sigma_i~U[.15,.35], corr 0.7 equicorr(.3) + 0.3 Wishart(d,d+2) "
                             "seed 11, 2^22 paths each, geometric-basket control variate",
                 "paths_per_step": self.units(), "contracts_per_step": len(self.cs)}
@@ -325,13 +325,13 @@ class LsmWorkload:
 
 class BinomWorkload:
     name = "binom"
-    metric = "contracts/sec (closed binomial sum, config 1)"
+    metric = "contracts/sec (closed binomial sum, 1024 contracts)"
     unit = "contracts/s"
     dominant = "binom_kernel"
 
     def __init__(self, rank):
         from parcompfin_gb300 import workloads
-        self.cs = workloads.config1()
+        self.cs = workloads.binom_book()
 
     def setup(self, ctx):
         pass
@@ -351,7 +351,7 @@ class BinomWorkload:
         return float(len(self.cs))
 
     def config(self):
-        return {"workload": "binom: config 1, 1024 contracts (seed 7), K~U[80,120], "
+        return {"workload": "binom: 1024 contracts (seed 7), K~U[80,120], "
                             "r~U[.01,.06], sigma~U[.1,.5], T~U[.25,2], call/put 50/50, "
                             "N~U{1000..200000}, reference rounding order",
                 "contracts_per_step": len(self.cs)}
@@ -403,7 +403,7 @@ class MixedWorkload:
         import parcompfin_gb300 as pcf
         from parcompfin_gb300 import workloads
         self.rank = rank
-        self.spec = workloads.config4(self.R, seed=17 + 1000 * rank)
+        self.spec = workloads.mixed_stream(self.R, seed=17 + 1000 * rank)
         self.base = [self._req(pcf, s, 0) for s in self.spec]
 
     @staticmethod
@@ -480,8 +480,8 @@ class MixedWorkload:
         kinds = {}
         for s in self.spec:
             kinds[s["kind"]] = kinds.get(s["kind"], 0) + 1
-        return {"workload": "mixed: config 4, 1000 requests per step (seed 17): 30% European "
-                            "(config-0 jittered), 20% basket d~U{2..32}, 30% Asian (config-3 "
+        return {"workload": "mixed: served request stream, 1000 requests per step (seed 17): 30% European "
+                            "(ATM call jittered), 20% basket d~U{2..32}, 30% Asian (Asian-book "
                             "distribution), 20% American put (LSM, 50 dates, N in 2^16..2^21); "
                             "each priced to a 5e-4 relative standard error with its control "
                             "variate",
@@ -519,7 +519,7 @@ class MixedWorkload:
         served = {}
         for rate in self.LOADS:
             n = int(min(4 * self.R, max(self.R, rate * 1.0)))
-            spec = workloads.config4(n, seed=29 + rate)
+            spec = workloads.mixed_stream(n, seed=29 + rate)
             reqs = [self._req(pcf, s, 0) for s in spec]
             arr = workloads.poisson_arrivals(n, rate, seed=31 + rate)
             out, st = pcf.serve_trace(reqs, arr, target_rel_se=self.TARGET, ctx=ctx)
@@ -614,7 +614,7 @@ class MixedWorkload:
 
 
 class AmerBatchWorkload:
-    """The American leg of config 4 alone: 64 puts, one cluster each."""
+    """The American leg of the mixed stream alone: 64 puts, one cluster each."""
     name = "amerbatch"
     metric = "MC paths/sec (American puts, batched Longstaff-Schwartz)"
     unit = "paths/s"
@@ -644,9 +644,9 @@ class AmerBatchWorkload:
         return float(self.C)
 
     def config(self):
-        return {"workload": "amerbatch: 64 American puts (config-4 distribution: K~U[90,110], "
-                            "sigma~U[.2,.4], r=.05, T=1, 50 dates), 2^16 paths each, one "
-                            "16-CTA cluster per contract",
+        return {"workload": "amerbatch: 64 American puts (the mixed stream's American "
+                            "distribution: K~U[90,110], sigma~U[.2,.4], r=.05, T=1, 50 "
+                            "dates), 2^16 paths each, one 8-CTA cluster per contract",
                 "paths_per_step": self.units(), "contracts_per_step": self.C}
 
     def roofline(self, ms, sms, mhz, peaks):

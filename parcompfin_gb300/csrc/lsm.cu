@@ -4,36 +4,47 @@
 // pathsfinder() of include/common.h:168-208 and the 3x3 solve of
 // include/common.h:98-141. The MPI build reduces the seven regression sums
 // and the in-the-money count to rank 0 and broadcasts three coefficients per
-// date (src/mc_amer_mpi.cpp:82-131). Here the same exchange is a grid-wide
-// FP64 reduction inside one persistent kernel.
+// date (src/mc_amer_mpi.cpp:82-131). Here the same exchange runs between the
+// CTAs of one launch, once per exercise date.
 //
-// One cooperative launch per contract, at most one 512-thread block per SM:
+// Two launch forms share one body (lsm_body):
+//   cooperative  one contract per launch, at most one 512-thread block per
+//                SM (pcf_mc_amer, and batch contracts too large for a
+//                cluster). Blocks exchange their partial sums through global
+//                memory and a bounded group barrier;
+//   cluster      many contracts per launch, one thread-block cluster per
+//                contract (pcf_plan_*). CTAs write their partial sums into
+//                every peer's shared memory and signal the peer's mbarrier.
+// Phases:
 //   forward   each thread generates its antithetic pairs (path p takes +z,
 //             path p + H takes -z, as pathsfinder pairs them) and writes
 //             S(date m), m = 1..M, to an FP32 time-major path matrix in HBM
 //             (row m-1; plus half at columns [0, Hp), minus half at
 //             [Hp, 2Hp), Hp = H rounded up to 4), coalesced across the warp;
-//   backward  for m = M-1..1: the block's slice of row m-1 (two contiguous
-//             runs) arrives in shared memory by TMA bulk copy. The copy for
-//             date m-1 is issued as soon as date m's has landed, so HBM
-//             latency hides behind the date's reduction and barrier. The
-//             block accumulates the 8 regression sums of its in-the-money
-//             paths, publishes one FP64 partial, waits at a bounded group
-//             barrier, reduces all partials in block order (every block gets
-//             the same bits), solves the normal equations by the adjugate
-//             formula and updates the exercise decision of its paths from the
-//             same shared-memory slice;
+//   backward  for m = M-1..1 the block's slice of row m-1 (two contiguous
+//             runs) arrives in shared memory by TMA bulk copy, issued two
+//             dates ahead. Each thread updates the exercise decision of its
+//             paths at date m and, in the same pass, adds date m-1's
+//             regression sums in FP32. A warp reduce-scatter leaves the
+//             warp's eight sums in eight lanes; after one block barrier a
+//             single warp adds the warp partials and then all CTAs' partials
+//             in double-float, in a fixed order (every CTA gets the same
+//             bits), widens them to FP64, solves the normal equations and
+//             publishes the coefficients before a second block barrier;
 //   final     discounted cash flows and the martingale control variate are
 //             averaged over antithetic pairs and reduced with the
 //             deterministic last-block finaliser (cooperative launch) or
 //             through distributed shared memory (cluster launch).
-// Per-path state (cash flow, exercise date) stays in shared memory for the
-// whole sweep. The regression basis is {1, x, x^2} with x = (S - E)/E: the
-// reference's S - E rescaled, the same fitted values in exact arithmetic.
+// Per-path state stays in shared memory for the whole sweep: the cash flow
+// discounted to time 0 (so a date's regression target is one multiply by the
+// date's growth factor) and the exercise date (8 bits where M <= 255). The
+// regression basis is {1, x, x^2} with x = (S - E)/E: the reference's S - E
+// rescaled, the same fitted values in exact arithmetic.
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -49,26 +60,26 @@ namespace pcf {
 namespace {
 
 constexpr int kLsmBlock = 512;
-constexpr int kRegSums = 8;  // n, x, x^2, x^3, x^4, y, y x, y x^2
-constexpr size_t kLsmMaxSmem = 227 * 1024;
+constexpr int kLsmWarps = kLsmBlock / 32;
+constexpr int kRegSums = 8;      // n, x, x^2, x^3, x^4, y, y x, y x^2
+constexpr int kMaxCluster = 16;  // CTAs per contract in a cluster launch
 
 struct LsmParams {
   float pf, nK, E, invE;  // payoff = max(pf S + nK, 0); x = (S - E) * invE
   float a2, b2, l2S0;     // per-date log2 drift / vol, log2 S0
-  float gdisc;            // exp(-rT)
   float rf, sigf, dtf;    // r, sigma, T/M: the European price of the control variate
   int M, ref_exercise;
   long long H;            // antithetic pairs = N / 2
   long long Hp;           // H rounded up to a multiple of 4
   int pairs_per_block;    // PB, a multiple of 4
-  int nblocks;
+  int nblocks;            // blocks (cooperative) or CTAs of the cluster
   uint32_t seed_lo, seed_hi, stream;
   unsigned wait_limit;       // group-barrier polls before giving up
-  unsigned copy_wait_limit;  // mbarrier polls before giving up on a bulk copy
+  unsigned copy_wait_limit;  // mbarrier polls before giving up
   float* paths;           // M rows of 2*Hp floats
-  const float* dtab;      // exp(-r dt k), k = 0..M
-  double* partial;        // 2 x nblocks x kRegSums
-  double* fpartial;       // nblocks x kMoments
+  const float* dtab;      // exp(-r dt k), k = 0..M, then exp(+r dt k), k = 0..M
+  double* partial;        // 2 x nblocks x kRegSums (cooperative)
+  double* fpartial;       // nblocks x kMoments (cooperative)
   unsigned* barrier;
   unsigned* ticket;
   int* err;               // 1: a barrier wait gave up, 2: a bulk copy wait gave up
@@ -100,7 +111,7 @@ __device__ float european_price(const LsmParams& P, float S, float rem) {
 // nine divisions. In exact arithmetic this is the reference's solution; FP64
 // is slow on GB300, so the short chain matters (it runs once per date on the
 // critical path).
-__device__ bool solve3(const double* a, double* coef) {
+__device__ __forceinline__ bool solve3(const double* a, double (&coef)[3]) {
   const double c00 = fma(a[2], a[4], -a[3] * a[3]);
   const double c01 = fma(a[2], a[3], -a[1] * a[4]);
   const double c02 = fma(a[1], a[3], -a[2] * a[2]);
@@ -117,36 +128,59 @@ __device__ bool solve3(const double* a, double* coef) {
   return true;
 }
 
+// Dynamic shared memory of one block: two copy mbarriers, the discount and
+// growth tables, per-path state, and two path-slice buffers.
+template <typename TauT>
 struct LsmSmem {
-  uint64_t* bar;           // 2 mbarriers
-  float* dt;               // M+1
-  float* cf;               // 2*PB
-  unsigned short* tau;     // 2*PB
-  float* buf[2];           // 2 x 2*PB path slices
+  uint64_t* bar;  // 2 mbarriers, one per slice buffer
+  float* dt;      // exp(-r dt k), k = 0..M
+  float* edt;     // exp(+r dt k), k = 0..M
+  float* cf;      // 2*PB cash flows, discounted to time 0
+  TauT* tau;      // 2*PB exercise dates
+  float* buf;     // 2 x 2*PB path slices, back to back
+  int PB;
+  __device__ __forceinline__ float* slice(int k) const { return buf + (size_t)k * 2 * PB; }
 };
 
-__device__ __forceinline__ LsmSmem carve(unsigned char* base, int PB, int M) {
-  LsmSmem s;
+__host__ __device__ __forceinline__ size_t r16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+template <typename TauT>
+__device__ __forceinline__ LsmSmem<TauT> carve(unsigned char* base, int PB, int M) {
+  LsmSmem<TauT> s;
   size_t o = 0;
   s.bar = (uint64_t*)(base + o);
   o += 16;
   s.dt = (float*)(base + o);
-  o += ((size_t)(M + 1) * 4 + 15) & ~(size_t)15;
+  o += r16((size_t)(M + 1) * 4);
+  s.edt = (float*)(base + o);
+  o += r16((size_t)(M + 1) * 4);
   s.cf = (float*)(base + o);
   o += (size_t)2 * PB * 4;
-  s.tau = (unsigned short*)(base + o);
-  o += ((size_t)2 * PB * 2 + 15) & ~(size_t)15;
-  s.buf[0] = (float*)(base + o);
-  o += (size_t)2 * PB * 4;
-  s.buf[1] = (float*)(base + o);
+  s.tau = (TauT*)(base + o);
+  o += r16((size_t)2 * PB * sizeof(TauT));
+  s.buf = (float*)(base + o);
+  s.PB = PB;
   return s;
 }
 
+// Static shared memory of one block: the exchange of regression sums.
+struct LsmShared {
+  float wpart[kLsmWarps][kRegSums];              // per-warp FP32 sums
+  alignas(16) DF xin[2][kMaxCluster][kRegSums];  // cluster: every CTA's totals, by date parity
+  alignas(16) DF ctot[kRegSums];                 // this CTA's totals
+  uint64_t xbar[2];                              // cluster: arrivals of the CTAs' totals
+  double t[kRegSums];                            // the contract's sums, FP64
+  float coef[3];
+  int mode;  // 0 skip the date, 1 few in-the-money paths, 2 regression
+  int fail;  // a wait gave up
+  DF sh[kLsmWarps * kMoments];
+  DF fin[kMoments];
+};
+
 // Bulk-copies the block's slice of row r (pairs [p0, p0 + nbr)) to dst:
 // plus half to dst[0..nbr), minus half to dst[PB..PB + nbr).
-__device__ __forceinline__ void issue_row(const LsmParams& P, const LsmSmem& S, int r,
-                                          long long p0, int nbr, int PB, float* dst,
-                                          uint64_t* bar) {
+__device__ __forceinline__ void issue_row(const LsmParams& P, int r, long long p0, int nbr, int PB,
+                                          float* dst, uint64_t* bar) {
   const float* row = P.paths + (size_t)r * 2 * P.Hp;
   const uint32_t bytes = (uint32_t)nbr * 4u;
   mbar_arrive_expect_tx(bar, 2u * bytes);
@@ -168,142 +202,167 @@ __device__ __forceinline__ void reg_accumulate(const LsmParams& P, float Sv, flo
   acc[7] = fmaf(y, x2, acc[7]);
 }
 
-// Block reduction of the regression sums for date m, the exchange of block
-// partials, the 3x3 solve, and the issue of the next bulk copy.
-//   cooperative launch (CLUSTER = false): each block publishes its partial in
-//     global memory, waits at the bounded group barrier, then every block
-//     sums all partials in block order (so all blocks get the same bits);
-//   cluster launch (CLUSTER = true, one cluster per contract): each CTA keeps
-//     its partial in shared memory; after a hardware cluster barrier every
-//     CTA reads all CTAs' partials through distributed shared memory, in
-//     rank order.
-// Leaves the date's mode and coefficients in shared memory. When `next_row`
-// >= 0, thread 0 issues the bulk copy of that row into `next_buf` once every
-// thread is past the slice that buffer held. Returns false if a bounded wait
-// gave up (cooperative launch only).
-template <bool CLUSTER>
-__device__ bool lsm_regress(const LsmParams& P, const LsmSmem& S, float (&acc)[kRegSums], int m,
-                            int b, DF* sh, DF (*red)[kRegSums], double* s_coef, int* s_mode,
-                            int next_row, long long p0, int nbr, int PB, float* next_buf,
-                            uint64_t* next_bar) {
-  DF v[kRegSums], tot[kRegSums];
+// Reduce-scatter of eight FP32 sums over a warp: each step sends half of the
+// lane's values to the partner lane and keeps the half the partner sends.
+// Afterwards the four lanes l with ((l >> 2) & 7) == q hold the warp total of
+// sum q. FP32 addition is commutative, so those lanes hold the same bits.
+__device__ __forceinline__ float warp_scatter8(const float (&a)[kRegSums]) {
+  const int lane = threadIdx.x & 31;
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  float v4[4], v2[2];
 #pragma unroll
-  for (int q = 0; q < kRegSums; ++q) v[q] = DF{acc[q], 0.f};
-  block_sum_df<kRegSums>(v, sh, tot);  // ends with __syncthreads: slices are free
-  float2* slot = (float2*)P.partial + (size_t)(m & 1) * P.nblocks * kRegSums;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int q = 0; q < kRegSums; ++q) {
-      if (CLUSTER) red[m & 1][q] = tot[q];
-      else slot[(size_t)b * kRegSums + q] = make_float2(tot[q].hi, tot[q].lo);
-    }
-    if (next_row >= 0 && nbr > 0) issue_row(P, S, next_row, p0, nbr, PB, next_buf, next_bar);
+  for (int i = 0; i < 4; ++i) {
+    const float send = b4 ? a[i] : a[i + 4];
+    const float keep = b4 ? a[i + 4] : a[i];
+    v4[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
   }
-  if (CLUSTER) {
-    cg::this_cluster().sync();
-  } else {
-    if (!group_barrier(P.barrier, (unsigned)P.nblocks, P.err, P.wait_limit)) return false;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float send = b3 ? v4[i] : v4[i + 2];
+    const float keep = b3 ? v4[i + 2] : v4[i];
+    v2[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
   }
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    DF g[kRegSums];
-#pragma unroll
-    for (int q = 0; q < kRegSums; ++q) g[q] = DF{0.f, 0.f};
-    if (CLUSTER) {
-      if (lane < P.nblocks) {
-        const DF* rr = cg::this_cluster().map_shared_rank(&red[m & 1][0], lane);
-#pragma unroll
-        for (int q = 0; q < kRegSums; ++q) g[q] = rr[q];
-      }
-    } else {
-      for (int bb = lane; bb < P.nblocks; bb += 32) {
-        const float4* r4 = (const float4*)(slot + (size_t)bb * kRegSums);
-        float4 a[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] = __ldcg(r4 + u);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          g[2 * u] = df_add(g[2 * u], DF{a[u].x, a[u].y});
-          g[2 * u + 1] = df_add(g[2 * u + 1], DF{a[u].z, a[u].w});
-        }
-      }
+  float v = (b2 ? v2[1] : v2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? v2[0] : v2[1], 4);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
+}
+
+// Cooperative launch: arrival at the group barrier by one thread, after the
+// block's partials were stored and fenced. `counter` only grows: arrival
+// number a (0-based) waits until the count reaches (a/G + 1)*G. Bounded: after
+// `limit` polls (or once another block reported a failure) it raises *err and
+// returns false.
+__device__ __forceinline__ bool group_arrive_wait(unsigned* counter, unsigned G, int* err,
+                                                  unsigned limit) {
+  const unsigned a = atomicAdd(counter, 1u);
+  const unsigned target = (a / G + 1u) * G;
+  for (unsigned polls = 0;; ++polls) {
+    const unsigned c = *((volatile unsigned*)counter);
+    if ((int)(c - target) >= 0) break;
+    if (*((volatile int*)err) != 0 || polls > limit) {
+      atomicExch(err, 1);
+      return false;
     }
-    double t[kRegSums];
-#pragma unroll
-    for (int q = 0; q < kRegSums; ++q) t[q] = df_value(warp_sum_df(g[q]));
-    if (lane == 0) {
-      if (t[0] == 0.0) {
-        *s_mode = 0;
-      } else if (t[0] <= 2.0) {
-        *s_mode = 1;
-      } else {
-        double c[3];
-        if (solve3(t, c)) {
-          *s_mode = 2;
-          s_coef[0] = c[0];
-          s_coef[1] = c[1];
-          s_coef[2] = c[2];
-        } else {
-          *s_mode = 0;
-          if (b == 0) atomicAdd(P.singular, 1);
-        }
-      }
-    }
+    __nanosleep(32);
   }
-  __syncthreads();
+  __threadfence();
   return true;
 }
 
-// Exercise decision of one path at date m (src/mc_amer.cpp:73-106).
-__device__ __forceinline__ void lsm_update(const LsmParams& P, const LsmSmem& S, int s, float Sv,
-                                           int m, int mode, float c0, float c1, float c2) {
-  const float pv = lsm_payoff(P, Sv);
-  if (pv > 0.f) {
-    float cont, ex = pv;
-    if (mode == 1) {
-      cont = S.cf[s] * S.dt[S.tau[s] - m];
-    } else {
-      const float x = (Sv - P.E) * P.invE;
-      cont = fmaf(fmaf(c2, x, c1), x, c0);
-      // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E).
-      if (P.ref_exercise) ex = fmaxf(P.pf * (Sv - 2.f * P.E), 0.f);
+// Date d's regression, run by warp 0 between the two block barriers: the
+// block's total of each sum, the exchange of block totals, the contract's
+// sums in FP64 and the solve. Leaves the mode and coefficients in X.
+template <bool CLUSTER>
+__device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared& X, int d, int b,
+                                             uint32_t& xph) {
+  const int lane = threadIdx.x & 31;
+  const int q = lane & 7;
+  // Block total of sum q: lane groups l>>3 = 0..3 each add four warps' sums,
+  // then two shuffle steps combine the groups. Lanes 0..7 hold the totals.
+  DF v = DF{X.wpart[lane >> 3][q], 0.f};
+#pragma unroll
+  for (int w = (lane >> 3) + 4; w < kLsmWarps; w += 4) v = df_add_f(v, X.wpart[w][q]);
+  v = df_add(v, shfl_xor_df(v, 8));
+  v = df_add(v, shfl_xor_df(v, 16));
+  const int slot = d & 1;
+  const int G = P.nblocks;
+  DF g{0.f, 0.f};
+  if (CLUSTER) {
+    // Every CTA writes its eight totals into xin[slot][b] of every CTA and
+    // arrives on that CTA's xbar[slot]. Slot reuse is safe: a CTA sends date
+    // d-2 only after its wait for date d-1, which needs every peer's date d-1
+    // totals, which each peer sends after reading its date d slot.
+    if (lane < kRegSums) X.ctot[lane] = v;
+    __syncwarp();
+    if (lane < G) {
+      const float4* src = reinterpret_cast<const float4*>(X.ctot);
+      const uint32_t dst = cluster_map(&X.xin[slot][b][0], (uint32_t)lane);
+#pragma unroll
+      for (int j = 0; j < kRegSums * 2 / 4; ++j) st_cluster_v4(dst + 16u * j, src[j]);
+      mbar_arrive_remote(cluster_map(&X.xbar[slot], (uint32_t)lane));
     }
-    if (ex > cont) {
-      S.cf[s] = ex;
-      S.tau[s] = (unsigned short)m;
+    if (!mbar_wait_cluster(&X.xbar[slot], (xph >> slot) & 1u, P.copy_wait_limit)) {
+      X.fail = 1;
+      atomicExch(P.err, 1);
     }
+    xph ^= 1u << slot;
+    for (int r = lane >> 3; r < G; r += 4) g = df_add(g, X.xin[slot][r][q]);
+  } else {
+    float2* part = (float2*)P.partial + (size_t)slot * G * kRegSums;
+    if (lane < kRegSums) {
+      part[(size_t)b * kRegSums + lane] = make_float2(v.hi, v.lo);
+      __threadfence();
+    }
+    __syncwarp();
+    int ok = 1;
+    if (lane == 0) ok = group_arrive_wait(P.barrier, (unsigned)G, P.err, P.wait_limit);
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok && lane == 0) X.fail = 1;
+#pragma unroll 4
+    for (int bb = lane >> 3; bb < G; bb += 4) {
+      const float2 p = __ldcg(part + (size_t)bb * kRegSums + q);
+      g = df_add(g, DF{p.x, p.y});
+    }
+  }
+  g = df_add(g, shfl_xor_df(g, 8));
+  g = df_add(g, shfl_xor_df(g, 16));
+  if (lane < kRegSums) X.t[lane] = df_value(g);
+  __syncwarp();
+  if (lane == 0) {
+    const double n = X.t[0];
+    int mode = 2;
+    double c[3] = {0.0, 0.0, 0.0};
+    if (n == 0.0) {
+      mode = 0;
+    } else if (n <= 2.0) {
+      mode = 1;
+    } else if (!solve3(X.t, c)) {
+      mode = 0;
+      if (b == 0) atomicAdd(P.singular, 1);
+    }
+    X.mode = mode;
+    X.coef[0] = (float)c[0];
+    X.coef[1] = (float)c[1];
+    X.coef[2] = (float)c[2];
   }
 }
 
 // One contract's forward pass, backward sweep and final moments, executed by
-// block `b` of the contract's `P.nblocks` blocks. In a cluster launch a
-// failed copy wait is recorded and the CTA keeps taking part in every cluster
-// barrier (a hardware barrier has no timeout), so no CTA leaves early.
-template <bool CLUSTER>
+// block `b` of the contract's `P.nblocks` blocks. Every wait is bounded. A
+// cooperative block that gave up leaves after its in-flight copies landed; a
+// cluster CTA records the failure and keeps taking part in every exchange and
+// cluster barrier (a hardware barrier has no timeout), so no CTA leaves early.
+template <bool CLUSTER, typename TauT>
 __device__ void lsm_body(const LsmParams& P, int b) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int PB = P.pairs_per_block;
   const int M = P.M;
-  const LsmSmem S = carve(smem_raw, PB, M);
-  __shared__ DF sh[32 * kRegSums];
-  __shared__ DF red[2][kRegSums];
-  __shared__ DF fin[kMoments];
-  __shared__ double s_coef[3];
-  __shared__ int s_mode;  // 0 skip date, 1 few ITM paths, 2 regression
-  __shared__ int s_ok;
+  const LsmSmem<TauT> S = carve<TauT>(smem_raw, PB, M);
+  __shared__ LsmShared X;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 
   const long long p0 = (long long)b * PB;
   const int nb = (int)max(0LL, min((long long)PB, P.H - p0));  // pairs in this block
   const int nbr = (nb + 3) & ~3;                                // bulk-copy width
-  for (int k = threadIdx.x; k <= M; k += kLsmBlock) S.dt[k] = P.dtab[k];
+  for (int k = threadIdx.x; k <= M; k += kLsmBlock) {
+    S.dt[k] = P.dtab[k];
+    S.edt[k] = P.dtab[M + 1 + k];
+  }
   if (threadIdx.x == 0) {
     mbar_init(&S.bar[0], 1);
     mbar_init(&S.bar[1], 1);
+    if (CLUSTER) {
+      mbar_init(&X.xbar[0], (uint32_t)P.nblocks);
+      mbar_init(&X.xbar[1], (uint32_t)P.nblocks);
+    }
     fence_mbar_init();
+    X.fail = 0;
   }
 
   // ---- forward: generate and store paths ----
   const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
+  const float dM = P.dtab[M];
   for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
     const long long p = p0 + i;
     float Lp = 0.f, Lm = 0.f, Sp = 0.f, Sm = 0.f;
@@ -319,82 +378,83 @@ __device__ void lsm_body(const LsmParams& P, int b) {
       row[p] = Sp;
       row[P.Hp + p] = Sm;
     }
-    S.cf[i] = lsm_payoff(P, Sp);
-    S.cf[PB + i] = lsm_payoff(P, Sm);
-    S.tau[i] = (unsigned short)M;
-    S.tau[PB + i] = (unsigned short)M;
+    S.cf[i] = lsm_payoff(P, Sp) * dM;
+    S.cf[PB + i] = lsm_payoff(P, Sm) * dM;
+    S.tau[i] = (TauT)M;
+    S.tau[PB + i] = (TauT)M;
   }
-  // The bulk copies below read what this block's threads just stored.
+  // The bulk copies below read what this block's threads just stored; the
+  // cluster barrier also publishes the exchange mbarriers to the peers.
   fence_proxy_async_global();
-  __syncthreads();
+  if (CLUSTER) cg::this_cluster().sync();
+  else __syncthreads();
 
-  // Buffer schedule: date d's slice sits in buf[(M - 1 - d) & 1]. Thread 0
-  // owns the copies; pending[k] says a copy into buf[k] is in flight.
-  bool pending[2] = {false, false};
-  uint32_t parity[2] = {0u, 0u};
-  bool alive = true;
-  auto wait_buf = [&](int k) {  // thread 0 only
-    if (!pending[k]) return true;
-    if (!mbar_wait(&S.bar[k], parity[k], P.copy_wait_limit)) return false;
-    parity[k] ^= 1u;
-    pending[k] = false;
-    return true;
-  };
-  if (threadIdx.x == 0) {
-    s_ok = 1;
-    if (nbr > 0) {
-      issue_row(P, S, M - 2, p0, nbr, PB, S.buf[0], &S.bar[0]);  // date M-1
-      pending[0] = true;
-      if (!wait_buf(0)) {
-        atomicExch(P.err, 2);
-        s_ok = 0;
-      }
+  // Buffer schedule: date d's slice sits in buf[(M - 1 - d) & 1]. Thread 32
+  // issues every copy; every thread waits on the copy it is about to read.
+  // `pend` (copies issued, not yet waited) and `ph` (mbarrier parities) evolve
+  // the same way in every thread.
+  uint32_t ph = 0, pend = 0, xph = 0;
+  if (nbr > 0) {
+    if (threadIdx.x == 32) {
+      issue_row(P, M - 2, p0, nbr, PB, S.slice(0), &S.bar[0]);                 // date M-1
+      if (M >= 3) issue_row(P, M - 3, p0, nbr, PB, S.slice(1), &S.bar[1]);  // date M-2
     }
+    pend = M >= 3 ? 3u : 1u;
   }
-  __syncthreads();
-  if (!CLUSTER) alive = s_ok != 0;
+  auto wait_copy = [&](int k) {
+    if (!((pend >> k) & 1u)) return;
+    if (!mbar_wait(&S.bar[k], (ph >> k) & 1u, P.copy_wait_limit)) {
+      X.fail = 1;
+      atomicExch(P.err, 2);
+    }
+    ph ^= 1u << k;
+    pend &= ~(1u << k);
+  };
+  // Regression for date d from each thread's sums; then thread 32 issues the
+  // copy of `next_row` into buf[next_k] (free: every thread has passed the
+  // first barrier, so it is done reading that buffer).
+  auto regress = [&](const float (&acc)[kRegSums], int d, int next_row, int next_k) {
+    const float v = warp_scatter8(acc);
+    if ((lane & 3) == 0) X.wpart[wid][lane >> 2] = v;
+    __syncthreads();
+    if (next_row >= 0 && nbr > 0) {
+      if (threadIdx.x == 32) issue_row(P, next_row, p0, nbr, PB, S.slice(next_k), &S.bar[next_k]);
+      pend |= 1u << next_k;
+    }
+    if (wid == 0) regress_date<CLUSTER>(P, X, d, b, xph);
+    __syncthreads();
+  };
 
   // Sums for date M-1 (the only date without a preceding update pass).
-  if (alive) {
+  {
+    wait_copy(0);
     float acc[kRegSums];
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
-    const float* sl = S.buf[0];
+    const float* sl = S.slice(0);
+    const float e1 = S.edt[M - 1];
     for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + i;
         const float Sv = sl[s];
-        if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * S.dt[S.tau[s] - (M - 1)], acc);
+        if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * e1, acc);
       }
     }
-    if (threadIdx.x == 0 && M - 2 >= 1 && nbr > 0) pending[1] = true;  // issued in lsm_regress
-    alive = lsm_regress<CLUSTER>(P, S, acc, M - 1, b, sh, red, s_coef, &s_mode,
-                                 M - 2 >= 1 ? M - 3 : -1, p0, nbr, PB, S.buf[1], &S.bar[1]);
+    regress(acc, M - 1, -1, 0);
   }
 
   // Date m: update with date m's coefficients, fused with the sums of date m-1.
-  for (int m = M - 1; m >= 1 && alive; --m) {
+  bool failed = !CLUSTER && X.fail;
+  for (int m = M - 1; m >= 1 && !failed; --m) {
     const int k = (M - 1 - m) & 1;
     const bool has_next = m > 1;
-    if (has_next) {
-      if (threadIdx.x == 0) {
-        s_ok = 1;
-        if (nbr > 0 && !wait_buf(k ^ 1)) {
-          atomicExch(P.err, 2);
-          s_ok = 0;
-        }
-      }
-      __syncthreads();
-      if (!s_ok && !CLUSTER) {
-        alive = false;
-        break;
-      }
-    }
-    const int mode = s_mode;
-    const float c0 = (float)s_coef[0], c1 = (float)s_coef[1], c2 = (float)s_coef[2];
-    const float* cur = S.buf[k];
-    const float* nxt = S.buf[k ^ 1];
+    if (has_next) wait_copy(k ^ 1);
+    const int mode = X.mode;
+    const float c0 = X.coef[0], c1 = X.coef[1], c2 = X.coef[2];
+    const float dm = S.dt[m], em = S.edt[m], e1 = S.edt[m - 1];
+    const float* cur = S.slice(k);
+    const float* nxt = S.slice(k ^ 1);
     float acc[kRegSums];
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
@@ -402,27 +462,42 @@ __device__ void lsm_body(const LsmParams& P, int b) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + i;
-        if (mode != 0) lsm_update(P, S, s, cur[s], m, mode, c0, c1, c2);
+        // Exercise decision at date m (src/mc_amer.cpp:73-106).
+        if (mode != 0) {
+          const float Sv = cur[s];
+          const float pv = lsm_payoff(P, Sv);
+          if (pv > 0.f) {
+            float cont, ex = pv;
+            if (mode == 1) {
+              cont = S.cf[s] * em;
+            } else {
+              const float x = (Sv - P.E) * P.invE;
+              cont = fmaf(fmaf(c2, x, c1), x, c0);
+              // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E).
+              if (P.ref_exercise) ex = fmaxf(P.pf * (Sv - 2.f * P.E), 0.f);
+            }
+            if (ex > cont) {
+              S.cf[s] = ex * dm;
+              S.tau[s] = (TauT)m;
+            }
+          }
+        }
         if (has_next) {
           const float Sv = nxt[s];
-          if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * S.dt[S.tau[s] - (m - 1)], acc);
+          if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * e1, acc);
         }
       }
     }
     if (!has_next) break;
-    // buf[k] (date m) is free once lsm_regress's block reduction has synced;
-    // date m-2 goes there.
-    const int next_row = m - 2 >= 1 ? m - 3 : -1;
-    if (threadIdx.x == 0 && next_row >= 0 && nbr > 0) pending[k] = true;
-    alive = lsm_regress<CLUSTER>(P, S, acc, m - 1, b, sh, red, s_coef, &s_mode, next_row, p0,
-                                 nbr, PB, S.buf[k], &S.bar[k]);
+    regress(acc, m - 1, m - 2 >= 1 ? m - 3 : -1, k);
+    failed = !CLUSTER && X.fail;
   }
   __syncthreads();
-  if (!alive) {
+  if (failed) {
     // Let any bulk copy this block issued land before the block exits.
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 32)
       for (int k = 0; k < 2; ++k)
-        if (pending[k]) mbar_wait(&S.bar[k], parity[k], P.copy_wait_limit);
+        if ((pend >> k) & 1u) mbar_wait(&S.bar[k], (ph >> k) & 1u, P.copy_wait_limit);
     return;
   }
 
@@ -442,17 +517,17 @@ __device__ void lsm_body(const LsmParams& P, int b) {
     for (int h = 0; h < 2; ++h) {
       const int s = h * PB + i;
       const int tau = S.tau[s];
-      const float cf = S.cf[s];
-      y2 += cf * S.dt[tau];
+      const float cfd = S.cf[s];  // cash flow discounted to time 0
+      y2 += cfd;
       float g;
       if (P.ref_exercise) {
         // The reference's exercise value does not identify S_tau: use the
         // discounted European payoff at T (mean: the same P_E(S0, T)).
         g = S.dt[M] * lsm_payoff(P, last[h * P.Hp + p0 + i]);
       } else if (tau == M) {
-        g = cf * S.dt[M];  // European payoff at T (cf is payoff(S_M)), discounted
+        g = cfd;  // the discounted European payoff at T
       } else {
-        const float St = P.E + P.pf * cf;
+        const float St = P.E + P.pf * (cfd * S.edt[tau]);
         g = S.dt[tau] * european_price(P, St, (float)(M - tau) * P.dtf);
       }
       g2 += g;
@@ -466,16 +541,16 @@ __device__ void lsm_body(const LsmParams& P, int b) {
   }
   DF v[kMoments] = {df_of(sy), df_of(syy), df_of(sg), df_of(sgg), df_of(syg)};
   DF tot[kMoments];
-  block_sum_df<kMoments>(v, sh, tot);
+  block_sum_df<kMoments>(v, X.sh, tot);
   if (CLUSTER) {
     if (threadIdx.x == 0)
-      for (int q = 0; q < kMoments; ++q) fin[q] = tot[q];
+      for (int q = 0; q < kMoments; ++q) X.fin[q] = tot[q];
     cg::this_cluster().sync();
     if (b == 0 && threadIdx.x == 0) {
       DF t[kMoments];
       for (int q = 0; q < kMoments; ++q) t[q] = DF{0.f, 0.f};
       for (int r = 0; r < P.nblocks; ++r) {
-        const DF* rf = cg::this_cluster().map_shared_rank(&fin[0], r);
+        const DF* rf = cg::this_cluster().map_shared_rank(&X.fin[0], r);
         for (int q = 0; q < kMoments; ++q) t[q] = df_add(t[q], rf[q]);
       }
       for (int q = 0; q < kMoments; ++q) P.out[q] = df_value(t[q]);
@@ -486,24 +561,26 @@ __device__ void lsm_body(const LsmParams& P, int b) {
   }
 }
 
-__global__ void __launch_bounds__(kLsmBlock) lsm_kernel(LsmParams P) {
-  lsm_body<false>(P, blockIdx.x);
+__global__ void __launch_bounds__(kLsmBlock, 1) lsm_kernel(LsmParams P) {
+  lsm_body<false, unsigned short>(P, blockIdx.x);
 }
 
 // Many contracts in one launch, one thread-block cluster per contract
-// (cluster size = the contracts' common block count).
-__global__ void __launch_bounds__(kLsmBlock) lsm_cluster_kernel(const LsmParams* __restrict__ cs) {
+// (cluster size = the contracts' common CTA count). Two CTAs per SM.
+template <typename TauT>
+__global__ void __launch_bounds__(kLsmBlock, 2) lsm_cluster_kernel(const LsmParams* __restrict__ cs) {
   __shared__ LsmParams sP;  // the contract's parameters, read from shared memory
   const unsigned rank = cg::this_cluster().block_rank();
   const int c = (int)(blockIdx.x / cg::this_cluster().num_blocks());
   if (threadIdx.x == 0) sP = cs[c];
   __syncthreads();
-  lsm_body<true>(sP, (int)rank);
+  lsm_body<true, TauT>(sP, (int)rank);
 }
 
-size_t lsm_smem(int PB, int M) {
-  return 16 + ((((size_t)M + 1) * 4 + 15) & ~(size_t)15) + (size_t)2 * PB * 4 +
-         (((size_t)2 * PB * 2 + 15) & ~(size_t)15) + (size_t)2 * 2 * PB * 4;
+// Dynamic shared memory of one block (the carve above).
+size_t lsm_smem(int PB, int M, size_t tau_bytes) {
+  return 16 + 2 * r16((size_t)(M + 1) * 4) + (size_t)2 * PB * 4 +
+         r16((size_t)2 * PB * tau_bytes) + (size_t)2 * 2 * PB * 4;
 }
 
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -521,7 +598,6 @@ void lsm_fill(LsmParams& P, double S0, double E, double r, double sigma, double 
   P.a2 = (float)((r - 0.5 * sigma * sigma) * dtd * log2e);
   P.b2 = (float)(sigma * sqrt(dtd) * log2e);
   P.l2S0 = (float)(log(S0) * log2e);
-  P.gdisc = (float)exp(-r * T);
   P.rf = (float)r;
   P.sigf = (float)sigma;
   P.dtf = (float)dtd;
@@ -532,26 +608,139 @@ void lsm_fill(LsmParams& P, double S0, double E, double r, double sigma, double 
   P.seed_lo = (uint32_t)seed;
   P.seed_hi = (uint32_t)(seed >> 32);
   P.stream = stream;
-  P.wait_limit = 1u << 22;       // ~64 ns sleep + an L2 round trip per poll: seconds
-  P.copy_wait_limit = 1u << 20;  // try_wait polls: far beyond a microsecond-scale copy
+  P.wait_limit = 1u << 22;       // ~32 ns sleep + an L2 round trip per poll: seconds
+  P.copy_wait_limit = 1u << 20;  // try_wait polls: far beyond a microsecond-scale wait
 }
 
+// Discount factors exp(-r dt k) then growth factors exp(+r dt k), k = 0..M.
+size_t dtab_bytes(int M) { return sizeof(float) * 2 * ((size_t)M + 1); }
 void dtab_fill(float* dst, double r, double T, int M) {
   const double dtd = T / M;
-  for (int k = 0; k <= M; ++k) dst[k] = (float)exp(-r * dtd * k);
+  for (int k = 0; k <= M; ++k) {
+    dst[k] = (float)exp(-r * dtd * k);
+    dst[M + 1 + k] = (float)exp(r * dtd * k);
+  }
 }
 
-constexpr size_t kStaticSmemReserve = 4096;  // lsm_body's static shared arrays
+// Shared-memory limits of the device and of the three kernels, queried once
+// per device; the kernels' dynamic shared-memory ceilings are raised to the
+// device maximum at the same time.
+struct LsmLimits {
+  size_t per_block = 0;  // opt-in maximum per block
+  size_t per_sm = 0;
+  size_t reserved = 0;   // per block, taken by the system
+  size_t stat_coop = 0, stat8 = 0, stat16 = 0;  // static shared memory of each kernel
+  int cl_max = 8;        // CTAs per cluster the device co-schedules (8 or 16)
+  int status = PCF_OK;
+};
+
+template <typename K>
+int lsm_kernel_setup(K kernel, size_t per_block, size_t* stat, bool cluster) {
+  cudaFuncAttributes fa;
+  int st = cuda_status(cudaFuncGetAttributes(&fa, kernel), "lsm kernel attributes");
+  if (st) return st;
+  *stat = fa.sharedSizeBytes;
+  st = cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(per_block - fa.sharedSizeBytes)),
+                   "lsm smem attribute");
+  if (!st)
+    st = cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          (int)cudaSharedmemCarveoutMaxShared),
+                     "lsm carveout attribute");
+  if (!st && cluster)
+    st = cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                          1),
+                     "lsm cluster attribute");
+  return st;
+}
+
+const LsmLimits& lsm_limits(const pcf_ctx* c) {
+  static std::mutex mu;
+  static LsmLimits cache[64];
+  static bool have[64] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  const int dev = c->device & 63;
+  LsmLimits& L = cache[dev];
+  if (have[dev]) return L;
+  int v = 0;
+  L.status = cuda_status(
+      cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
+  L.per_block = (size_t)v;
+  if (!L.status)
+    L.status = cuda_status(
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device),
+        "attr");
+  L.per_sm = (size_t)v;
+  if (!L.status)
+    L.status = cuda_status(
+        cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, c->device), "attr");
+  L.reserved = (size_t)v;
+  if (!L.status) L.status = lsm_kernel_setup(lsm_kernel, L.per_block, &L.stat_coop, false);
+  if (!L.status)
+    L.status = lsm_kernel_setup(lsm_cluster_kernel<unsigned char>, L.per_block, &L.stat8, true);
+  if (!L.status)
+    L.status = lsm_kernel_setup(lsm_cluster_kernel<unsigned short>, L.per_block, &L.stat16, true);
+  if (!L.status) {
+    // 16-CTA clusters where the device can co-schedule them at two CTAs per
+    // SM with 4096-pair slices; otherwise the portable 8.
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(kLsmBlock);
+    cfg.dynamicSmemBytes = lsm_smem(4096, 64, 1);
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    L.cl_max = cudaOccupancyMaxActiveClusters(&n, lsm_cluster_kernel<unsigned char>, &cfg) ==
+                           cudaSuccess &&
+                       n > 0
+                   ? 16
+                   : 8;
+    cudaGetLastError();
+  }
+  have[dev] = L.status == PCF_OK;
+  return L;
+}
+
+bool lsm_fits(const LsmLimits& Lm, int PB, int M, size_t tau_bytes, size_t stat, int per_sm) {
+  const size_t need = lsm_smem(PB, M, tau_bytes) + stat;
+  return need <= Lm.per_block && (size_t)per_sm * (need + Lm.reserved) <= Lm.per_sm;
+}
 
 // Cooperative-launch grid for one contract: at most one block per SM, at
-// least one pair per thread. Returns false if it cannot be co-resident.
-bool coop_shape(const pcf_ctx* c, long long H, int M, int& G, int& PB, size_t& smem) {
+// least one pair per thread. Returns false if a block's slice does not fit.
+bool coop_shape(const pcf_ctx* c, const LsmLimits& Lm, long long H, int M, int& G, int& PB,
+                size_t& smem) {
   const long long G0 = std::max(1LL, std::min((H + kLsmBlock - 1) / kLsmBlock,
                                               (long long)c->sm_count));
   PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
   G = (int)((H + PB - 1) / PB);
-  smem = lsm_smem(PB, M);
-  return smem + kStaticSmemReserve <= kLsmMaxSmem;
+  smem = lsm_smem(PB, M, 2);
+  return lsm_fits(Lm, PB, M, 2, Lm.stat_coop, 1);
+}
+
+constexpr int kLsmPB[] = {512, 1024, 2048, 4096, 8192};
+constexpr int kNumPB = 5;
+
+// Shape of a contract in a cluster launch: the smallest power-of-two cluster
+// that covers the contract with slices that let two CTAs share an SM (the
+// smallest such slice at that cluster size); beyond that, the largest cluster
+// with one CTA per SM. Few CTAs per contract leave room for more contracts in
+// flight, and each CTA pays the per-date exchange once for more paths.
+bool cluster_shape(const LsmLimits& Lm, long long H, int M, int& cl, int& k, bool& t8) {
+  t8 = M <= 255;
+  const size_t tb = t8 ? 1 : 2, stat = t8 ? Lm.stat8 : Lm.stat16;
+  for (cl = 1; cl <= Lm.cl_max; cl *= 2)
+    for (k = 0; k < kNumPB; ++k)
+      if ((long long)cl * kLsmPB[k] >= H && lsm_fits(Lm, kLsmPB[k], M, tb, stat, 2)) return true;
+  cl = Lm.cl_max;
+  for (k = 0; k < kNumPB; ++k)
+    if ((long long)cl * kLsmPB[k] >= H && lsm_fits(Lm, kLsmPB[k], M, tb, stat, 1)) return true;
+  return false;
 }
 
 }  // namespace
@@ -583,6 +772,7 @@ void fill_amer_result(const double* s, long long N, double S0, double E, double 
 
 struct LsmCluster {  // one cluster launch: every contract with the same shape
   int CL = 0, PB = 0, C = 0;
+  bool t8 = true;
   size_t smem = 0;
   LsmParams* d_params = nullptr;
 };
@@ -596,40 +786,10 @@ struct LsmBatch {
   size_t bytes = 0;
 };
 
-int lsm_cluster_size(pcf_ctx* c) {
-  // 16 CTAs per cluster where the device can co-schedule them, else 8.
-  static int cached = 0;
-  if (cached) return cached;
-  cudaFuncSetAttribute(lsm_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  const size_t smem = lsm_smem(8192, 64);
-  cudaFuncSetAttribute(lsm_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = 16;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3(16);
-  cfg.blockDim = dim3(kLsmBlock);
-  cfg.dynamicSmemBytes = smem;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, lsm_cluster_kernel, &cfg) == cudaSuccess && n > 0)
-    cached = 16;
-  else
-    cached = 8;
-  cudaGetLastError();
-  (void)c;
-  return cached;
-}
-
 // Shapes and device layout of a batch: params tables | discount tables (the
 // uploaded prefix) | cooperative scratch | path matrices.
 struct LsmLayout {
-  std::vector<int> cls;  // index into kLsmPB, or -1 for the cooperative kernel
-  std::vector<int> cl;   // CTAs per contract (cluster size)
+  std::vector<int> group;  // launch group of each contract, -1: cooperative kernel
   std::vector<std::vector<int>> members;
   std::vector<size_t> o_params, o_dt, o_paths, o_coop;
   std::vector<int> coop_G, coop_PB;
@@ -637,37 +797,28 @@ struct LsmLayout {
   size_t upload = 0, total = 0;
 };
 
-constexpr int kLsmPB[] = {512, 1024, 2048, 4096, 8192};
+// Launch group of a cluster shape: (log2 cluster size, slice class, tau width).
+constexpr int kLsmGroups = 5 * kNumPB * 2;
+int group_of(int cl, int k, bool t8) {
+  int lg = 0;
+  while ((1 << lg) < cl) ++lg;
+  return (lg * kNumPB + k) * 2 + (t8 ? 1 : 0);
+}
 
 int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
+  const LsmLimits& Lm = lsm_limits(c);
+  if (Lm.status) return Lm.status;
   const size_t n = reqs.size();
-  // Shape of each contract: a cluster of the device's full size (16 CTAs
-  // where allowed), with the smallest slice class that covers the contract.
-  // Small slices keep each CTA's shared memory low, so two CTAs share an SM
-  // and more contracts are in flight; a contract too large for a cluster
-  // runs the cooperative kernel.
-  const int CLmax = lsm_cluster_size(c);
-  L.cls.assign(n, -1);
-  L.cl.assign(n, 0);
+  L.group.assign(n, -1);
+  L.members.assign(kLsmGroups, {});
   for (size_t i = 0; i < n; ++i) {
-    const long long H = reqs[i].N / 2;
-    const int cl = CLmax;
-    for (int k = 0; k < 5; ++k)
-      if ((long long)cl * kLsmPB[k] >= H &&
-          lsm_smem(kLsmPB[k], reqs[i].M) + kStaticSmemReserve <= kLsmMaxSmem) {
-        L.cls[i] = k;
-        L.cl[i] = cl;
-        break;
-      }
-  }
-  // Launch groups: one per (cluster size, slice class).
-  L.members.assign(5 * 5, {});
-  for (size_t i = 0; i < n; ++i)
-    if (L.cls[i] >= 0) {
-      int lg = 0;
-      while ((1 << lg) < L.cl[i]) ++lg;
-      L.members[lg * 5 + L.cls[i]].push_back((int)i);
+    int cl, k;
+    bool t8;
+    if (cluster_shape(Lm, reqs[i].N / 2, reqs[i].M, cl, k, t8)) {
+      L.group[i] = group_of(cl, k, t8);
+      L.members[L.group[i]].push_back((int)i);
     }
+  }
   size_t off = 0;
   L.o_params.assign(L.members.size(), 0);
   for (size_t k = 0; k < L.members.size(); ++k) {
@@ -677,7 +828,7 @@ int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
   L.o_dt.assign(n, 0);
   for (size_t i = 0; i < n; ++i) {
     L.o_dt[i] = off;
-    off = a256(off + sizeof(float) * (reqs[i].M + 1));
+    off = a256(off + dtab_bytes(reqs[i].M));
   }
   L.upload = off;
   L.coop_G.assign(n, 0);
@@ -685,8 +836,8 @@ int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
   L.coop_sm.assign(n, 0);
   L.o_coop.assign(n, 0);
   for (size_t i = 0; i < n; ++i) {
-    if (L.cls[i] >= 0) continue;
-    if (!coop_shape(c, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i], L.coop_sm[i]))
+    if (L.group[i] >= 0) continue;
+    if (!coop_shape(c, Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i], L.coop_sm[i]))
       return set_error(PCF_EINVAL, "American request with N = %lld is too large", reqs[i].N);
     L.o_coop[i] = off;  // partial (2 G 8 float2) | fpartial (G 5 float2) | 2 counters
     off = a256(off + 8 * (2 * (size_t)L.coop_G[i] * kRegSums + (size_t)L.coop_G[i] * kMoments) +
@@ -756,27 +907,28 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
     P.err = q.d_flags;
     P.singular = q.d_flags + 1;
   };
-  for (size_t k = 0; k < Lo.members.size(); ++k) {
-    if (Lo.members[k].empty()) continue;
+  for (size_t g = 0; g < Lo.members.size(); ++g) {
+    if (Lo.members[g].empty()) continue;
     LsmCluster L;
-    L.CL = 1 << (k / 5);
-    L.PB = kLsmPB[k % 5];
-    L.C = (int)Lo.members[k].size();
+    L.t8 = (g & 1) != 0;
+    L.PB = kLsmPB[(g / 2) % kNumPB];
+    L.CL = 1 << (g / 2 / kNumPB);
+    L.C = (int)Lo.members[g].size();
     int Mmax = 2;
-    LsmParams* tab = (LsmParams*)(h + Lo.o_params[k]);
+    LsmParams* tab = (LsmParams*)(h + Lo.o_params[g]);
     for (int j = 0; j < L.C; ++j) {
-      const int i = Lo.members[k][j];
+      const int i = Lo.members[g][j];
       fill(i, tab[j]);
       tab[j].pairs_per_block = L.PB;
       tab[j].nblocks = L.CL;
       Mmax = std::max(Mmax, reqs[i].M);
     }
-    L.smem = lsm_smem(L.PB, Mmax);
-    L.d_params = (LsmParams*)(d + Lo.o_params[k]);
+    L.smem = lsm_smem(L.PB, Mmax, L.t8 ? 1 : 2);
+    L.d_params = (LsmParams*)(d + Lo.o_params[g]);
     B->clusters.push_back(L);
   }
   for (size_t i = 0; i < reqs.size(); ++i) {
-    if (Lo.cls[i] >= 0) continue;
+    if (Lo.group[i] >= 0) continue;
     LsmParams P;
     fill(i, P);
     P.pairs_per_block = Lo.coop_PB[i];
@@ -805,11 +957,6 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
 int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
   int st;
   for (const LsmCluster& L : B->clusters) {
-    st = cuda_status(cudaFuncSetAttribute(lsm_cluster_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)L.smem),
-                     "lsm cluster smem attribute");
-    if (st) return st;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -822,8 +969,9 @@ int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
     cfg.stream = s;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    st = cuda_status(cudaLaunchKernelEx(&cfg, lsm_cluster_kernel,
-                                        (const LsmParams*)L.d_params),
+    const LsmParams* prm = L.d_params;
+    st = cuda_status(L.t8 ? cudaLaunchKernelEx(&cfg, lsm_cluster_kernel<unsigned char>, prm)
+                          : cudaLaunchKernelEx(&cfg, lsm_cluster_kernel<unsigned short>, prm),
                      "lsm cluster launch");
     if (st) return st;
     c->launches += 1;
@@ -831,10 +979,6 @@ int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
   for (size_t i = 0; i < B->coop.size(); ++i) {
     LsmParams& P = B->coop[i];
     st = cuda_status(cudaMemsetAsync(P.barrier, 0, 2 * sizeof(unsigned), s), "memset LSM counters");
-    if (st) return st;
-    st = cuda_status(cudaFuncSetAttribute(lsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)B->coop_smem[i]),
-                     "lsm smem attribute");
     if (st) return st;
     void* args[] = {&P};
     st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_kernel, dim3(B->coop_grid[i]),
@@ -866,14 +1010,12 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if (st) return st;
   pcf_ctx* c = resolve_ctx(ctx, &st);
   if (!c) return st;
+  const LsmLimits& Lm = lsm_limits(c);
+  if (Lm.status) return Lm.status;
   int G = 0, PB = 0;
   size_t smem = 0;
-  if (!coop_shape(c, N / 2, M, G, PB, smem))
+  if (!coop_shape(c, Lm, N / 2, M, G, PB, smem))
     return set_error(PCF_EINVAL, "N = %lld is too large for one device sweep", N);
-  st = cuda_status(cudaFuncSetAttribute(lsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem),
-                   "lsm smem attribute");
-  if (st) return st;
   int occ = 0;
   st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_kernel, kLsmBlock, smem),
                    "occupancy(lsm)");
@@ -900,7 +1042,7 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   }
   // Scratch: dtab | partial | fpartial | counters | out.
   const size_t o_dt = 0;
-  const size_t o_part = a256(o_dt + sizeof(float) * (M + 1));
+  const size_t o_part = a256(o_dt + dtab_bytes(M));
   const size_t o_fpart = a256(o_part + sizeof(double) * 2 * G * kRegSums);
   const size_t o_cnt = a256(o_fpart + sizeof(double) * G * kMoments);
   const size_t o_out = a256(o_cnt + sizeof(unsigned) * 4);
@@ -910,8 +1052,8 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   char* d = (char*)c->d_buf;
   char* h = (char*)c->h_buf;
   dtab_fill((float*)(h + o_dt), r, T, M);
-  st = cuda_status(cudaMemcpyAsync(d + o_dt, h + o_dt, sizeof(float) * (M + 1),
-                                   cudaMemcpyHostToDevice, c->stream), "H2D dtab");
+  st = cuda_status(cudaMemcpyAsync(d + o_dt, h + o_dt, dtab_bytes(M), cudaMemcpyHostToDevice,
+                                   c->stream), "H2D dtab");
   if (!st) st = cuda_status(cudaMemsetAsync(d + o_cnt, 0, sizeof(unsigned) * 4, c->stream),
                             "memset counters");
   if (st) return st;

@@ -125,6 +125,19 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
   return DF{hi, e - (hi - s)};
 }
 
+__device__ __forceinline__ DF df_add_f(DF a, float b) {  // df_add(a, {b, 0})
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b - bb);
+  e += a.lo;
+  const float hi = s + e;
+  return DF{hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ DF shfl_xor_df(DF v, int o) {
+  return DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
 __device__ __forceinline__ DF df_of(const KSum& k) {  // k.s - k.c, exactly
   const float s = k.s, m = -k.c;
   const float hi = s + m;
@@ -304,6 +317,43 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// ---- exchanges between the CTAs of a thread-block cluster ----
+// Address of the same shared-memory object in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_map(const void* p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, float4 v) {
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x),
+               "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+// Arrives on an mbarrier of another CTA of the cluster; releases this
+// thread's earlier shared::cluster stores to whoever completes the wait.
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t bar_cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(
+                   bar_cluster_addr)
+               : "memory");
+}
+// mbar_wait with cluster-scope acquire: the waiting thread sees what the
+// arriving threads of other CTAs stored before their arrive. Bounded.
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity,
+                                                  uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
         : "r"(smem_u32(bar)), "r"(parity)

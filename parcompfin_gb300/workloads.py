@@ -1,15 +1,14 @@
-"""Synthetic request sets with the shapes of the reference's benchmark configs.
+"""Synthetic request sets with the shapes of the reference's benchmark runs.
 
 Each generator is seeded, so every run prices the same requests. There is no
 public dataset: the reference's experiments are parameter sweeps
-(runscript_*.sh), and these sets follow the five benchmark configurations of
-the engine's acceptance tests.
+(runscript_*.sh), and these sets follow five benchmark workloads:
 
-  config0()  European call, S0=K=100, r=.05, sigma=.2, T=1 (mc_eur)
-  config1()  1024 closed-binomial contracts, uneven N (binom_embar)
-  config2()  baskets of 4, 16, 64 assets, Wishart-blended correlation (mc_eur_multi)
-  config3()  256 Asian contracts, M in {12, 52, 252}, N log-uniform (mc_asia)
-  config4()  the mixed request stream: European / basket / Asian / American
+  eur_contract()  European call, S0=K=100, r=.05, sigma=.2, T=1 (mc_eur)
+  binom_book()    1024 closed-binomial contracts, uneven N (binom_embar)
+  basket_book()   baskets of 4, 16, 64 assets, Wishart-blended correlation (mc_eur_multi)
+  asian_book()    256 Asian contracts, M in {12, 52, 252}, N log-uniform (mc_asia)
+  mixed_stream()  the mixed request stream: European / basket / Asian / American
 """
 from __future__ import annotations
 
@@ -19,11 +18,11 @@ import random
 import numpy as np
 
 
-def config0(N: int = 1_000_000, seed: int = 42) -> dict:
+def eur_contract(N: int = 1_000_000, seed: int = 42) -> dict:
     return dict(S0=100.0, E=100.0, r=0.05, sigma=0.2, T=1.0, N=N, payoff_fun=1, seed=seed)
 
 
-def config1(n: int = 1024, seed: int = 7) -> list:
+def binom_book(n: int = 1024, seed: int = 7) -> list:
     """(S0, E, r, sigma, T, N, payoff_fun) for the closed binomial sum."""
     rng = random.Random(seed)
     out = []
@@ -49,7 +48,7 @@ def wishart_corr(d: int, seed: int = 11) -> np.ndarray:
     return C
 
 
-def config2(dims=(4, 16, 64), N: int = 1 << 22, seed: int = 11) -> list:
+def basket_book(dims=(4, 16, 64), N: int = 1 << 22, seed: int = 11) -> list:
     """Basket calls, equal weights, S0_i = 100, K = 100, r = .03, T = 1."""
     rng = random.Random(seed)
     out = []
@@ -61,7 +60,7 @@ def config2(dims=(4, 16, 64), N: int = 1 << 22, seed: int = 11) -> list:
     return out
 
 
-def config3(n: int = 256, seed: int = 13) -> list:
+def asian_book(n: int = 256, seed: int = 13) -> list:
     """Asian fixed-strike arithmetic calls, r = .04."""
     rng = random.Random(seed)
     out = []
@@ -72,9 +71,9 @@ def config3(n: int = 256, seed: int = 13) -> list:
     return out
 
 
-def config4(n: int, seed: int = 17) -> list:
-    """The mixed request stream: 30% European (config-0 parameters jittered),
-    20% basket (d ~ U{2..32}), 30% Asian (config-3 distribution), 20%
+def mixed_stream(n: int, seed: int = 17) -> list:
+    """The mixed request stream: 30% European (the eur_contract parameters jittered),
+    20% basket (d ~ U{2..32}), 30% Asian (the asian_book distribution), 20%
     American put by Longstaff-Schwartz (S0 = 100, K ~ U[90,110], r = .05,
     sigma ~ U[.2,.4], T = 1, 50 exercise dates)."""
     rng = random.Random(seed)

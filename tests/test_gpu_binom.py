@@ -62,7 +62,7 @@ def test_reference_mode_random_contracts_vs_oracle(orc, ctx):
 
 @pytest.mark.parametrize("N", [199_999, 200_000])
 def test_reference_mode_large_n_vs_windowed_oracle(orc, ctx, N):
-    """At the largest config-1 N the full O(N^2) oracle is too slow; the
+    """At the largest binomial-book N the full O(N^2) oracle is too slow; the
     oracle's windowed restatement runs the same exact comb() chain for every
     pair index near N/2 (where all of the weight is)."""
     from parcompfin_gb300 import binom_embar

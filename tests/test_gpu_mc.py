@@ -59,7 +59,7 @@ def test_plain_and_cv_launches_share_the_payoff_sums(ctx):
     assert list(a.sums[:2]) == list(b.sums[:2])
 
 
-def test_eur_config0_against_black_scholes(ctx):
+def test_eur_atm_call_against_black_scholes(ctx):
     from parcompfin_gb300 import mc_eur_result
     bs = 10.450583572185565
     res = mc_eur_result(100, 100, .05, .2, 1.0, 1_000_000, "call", seed=42, use_cv=True, ctx=ctx)

@@ -20,7 +20,7 @@ TARGET = 5e-4
 
 def _trace(pcf, n, rate, seed):
     from parcompfin_gb300 import workloads
-    spec = workloads.config4(n, seed=seed)
+    spec = workloads.mixed_stream(n, seed=seed)
     reqs = []
     for s in spec:
         kw = dict(use_cv=True, seed=99, stream=s["id"])
