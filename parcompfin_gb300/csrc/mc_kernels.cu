@@ -93,7 +93,8 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
   }
 }
 
-// Asian: one path per thread; increment m uses lane m%4 of Philox block
+// Asian: item j covers paths [j*U, (j+1)*U), U = units_per_item, U/256 per
+// thread (path j*U + k*256 + thread); increment m uses lane m%4 of Philox block
 // (x=path, y=m/4). log2(S/S0) is accumulated, S = S0 * 2^L.
 // mode 0 (reference, src/mc_asia.cpp:31-35): I += S_m (c1 + c2 z_m) with S_m
 //   the level before the step; A = I/M.
@@ -103,46 +104,49 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
 // mode 1 equal weights 1/M on S_1..S_M.
 template <bool CV>
 __device__ __forceinline__ void asia_item(const McContract& C, int j, Moments<CV>& mo) {
-  const long long n = (long long)j * C.units_per_item + threadIdx.x;
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_ASIA};
   const int M = C.M;
   const float w = 1.f / (float)M;
-  float L = 0.f, I = 0.f, lg = 0.f;
-  for (int m0 = 0; m0 < M; m0 += 4) {
-    const float4 z = normals4(draw_words(key, (uint64_t)n, (uint32_t)(m0 >> 2)));
+  const int ppt = C.units_per_item / kBlock;
+#pragma unroll 1
+  for (int k = 0; k < ppt; ++k) {
+    const long long n = (long long)j * C.units_per_item + (long long)k * kBlock + threadIdx.x;
+    if (n >= C.N) break;
+    float L = 0.f, I = 0.f, lg = 0.f;
+    for (int m0 = 0; m0 < M; m0 += 4) {
+      const float4 z = normals4(draw_words(key, (uint64_t)n, (uint32_t)(m0 >> 2)));
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
-      const int m = m0 + l;
-      if (m < M) {
-        const float zl = lane4(z, l);
-        if (C.mode == 0) {
-          const float S = C.S0 * ex2_approx(L);
-          I = fmaf(S, fmaf(C.c2, zl, C.c1), I);
-          L += fmaf(C.b2, zl, C.a2);
-          if (CV) lg = fmaf(m == M - 1 ? C.w_last : w, L, lg);
-        } else {
-          L += fmaf(C.b2, zl, C.a2);
-          I += C.S0 * ex2_approx(L);
-          if (CV) lg = fmaf(w, L, lg);
+      for (int l = 0; l < 4; ++l) {
+        const int m = m0 + l;
+        if (m < M) {
+          const float zl = lane4(z, l);
+          if (C.mode == 0) {
+            const float S = C.S0 * ex2_approx(L);
+            I = fmaf(S, fmaf(C.c2, zl, C.c1), I);
+            L += fmaf(C.b2, zl, C.a2);
+            if (CV) lg = fmaf(m == M - 1 ? C.w_last : w, L, lg);
+          } else {
+            L += fmaf(C.b2, zl, C.a2);
+            I += C.S0 * ex2_approx(L);
+            if (CV) lg = fmaf(w, L, lg);
+          }
         }
       }
     }
+    const float Y = payoff(C, I * w);
+    const float G = CV ? payoff(C, C.S0 * ex2_approx(lg)) : 0.f;
+    mo.add(Y, G);
   }
-  const bool ok = n < C.N;
-  const float Y = ok ? payoff(C, I * w) : 0.f;
-  const float G = (CV && ok) ? payoff(C, C.S0 * ex2_approx(lg)) : 0.f;
-  mo.add(Y, G);
 }
 
-// Basket of d <= DMAX assets: one path per thread. Asset a's normal is lane
-// a%4 of Philox block (x=path, y=a/4). x = Lz with the correlation factor
-// staged in shared memory; log2 S_a = l0_a + v_a x_a; y = payoff(mean_a S_a),
+// Basket of d <= DMAX assets, one path. Asset a's normal is lane a%4 of
+// Philox block (x=path, y=a/4). x = Lz with the correlation factor staged in
+// shared memory; log2 S_a = l0_a + v_a x_a; y = payoff(mean_a S_a),
 // g = payoff(2^(mean_a log2 S_a)). mode 0: the factor is lower triangular
 // (Cholesky); mode 1: a full factor (eigen-decomposition fallback).
 template <int DMAX, bool CV>
-__device__ __forceinline__ void basket_item(const McContract& C, int j, const float* fb,
+__device__ __forceinline__ void basket_path(const McContract& C, const float* fb, long long n,
                                             Moments<CV>& mo) {
-  const long long n = (long long)j * C.units_per_item + threadIdx.x;
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_BASKET};
   const int d = C.M;
   const float* l0 = fb;
@@ -188,10 +192,29 @@ __device__ __forceinline__ void basket_item(const McContract& C, int j, const fl
     }
   }
   const float inv_d = 1.f / (float)d;
-  const bool ok = n < C.N;
-  const float Y = ok ? payoff(C, bsk * inv_d) : 0.f;
-  const float G = (CV && ok) ? payoff(C, ex2_approx(geo * inv_d)) : 0.f;
+  const float Y = payoff(C, bsk * inv_d);
+  const float G = CV ? payoff(C, ex2_approx(geo * inv_d)) : 0.f;
   mo.add(Y, G);
+}
+
+// Basket item j covers paths [j*U, (j+1)*U), U = units_per_item: U/256 paths
+// per thread (path j*U + k*256 + thread) for baskets of up to 8 assets, one
+// path per thread for larger ones (their path loop would hold the whole
+// unrolled factor product in registers).
+template <int DMAX, bool CV>
+__device__ __forceinline__ void basket_item(const McContract& C, int j, const float* fb,
+                                            Moments<CV>& mo) {
+  const long long n0 = (long long)j * C.units_per_item + threadIdx.x;
+  if (DMAX <= 8) {
+    const int ppt = C.units_per_item / kBlock;
+    for (int k = 0; k < ppt; ++k) {
+      const long long n = n0 + (long long)k * kBlock;
+      if (n >= C.N) break;
+      basket_path<DMAX, CV>(C, fb, n, mo);
+    }
+  } else if (n0 < C.N) {
+    basket_path<DMAX, CV>(C, fb, n0, mo);
+  }
 }
 
 __device__ __forceinline__ int find_contract(const int* start, int n, int item) {
@@ -204,45 +227,70 @@ __device__ __forceinline__ int find_contract(const int* start, int n, int item) 
   return lo;
 }
 
+// Persistent launch: blocks take work items from a queue in increasing
+// order. The next ticket is taken while the current item runs, and the item's
+// contract is found in one round: the contract is the block's previous one or
+// one of the next 255, so each thread tests one candidate (a binary search
+// covers longer jumps).
 template <int METHOD, int DMAX, bool CV>
 __global__ void __launch_bounds__(kBlock) mc_kernel(McLaunch L) {
   __shared__ DF sh[32 * kMoments];
-  __shared__ int s_item;
+  __shared__ int s_item[2];
+  __shared__ int s_c;
   extern __shared__ float s_fb[];
+  if (threadIdx.x == 0) {
+    s_c = -1;
+    if (L.persistent) s_item[0] = (int)atomicAdd(L.queue, 1u);
+  }
+  __syncthreads();
+  int c = 0;        // contract of the block's previous item
+  int loaded = -1;  // basket whose factor block sits in s_fb
   for (int iter = 0;; ++iter) {
     int item;
     if (L.persistent) {
-      if (threadIdx.x == 0) s_item = (int)atomicAdd(L.queue, 1u);
-      __syncthreads();
-      item = s_item;
-      __syncthreads();
+      item = s_item[iter & 1];
+      // Read by every thread after this item's barriers; the slot it
+      // overwrites was last read before the previous item's final barrier.
+      if (threadIdx.x == 0 && item < L.total_items)
+        s_item[(iter + 1) & 1] = (int)atomicAdd(L.queue, 1u);
     } else {
       if (iter > 0) break;
       item = blockIdx.x;
     }
     if (item >= L.total_items) break;
-    const int c = find_contract(L.item_start, L.ncontracts, item);
+    {
+      const int t = c + (int)threadIdx.x;
+      if (t < L.ncontracts && __ldg(L.item_start + t) <= item &&
+          (t + 1 == L.ncontracts || item < __ldg(L.item_start + t + 1)))
+        s_c = t;
+      __syncthreads();
+      const int found = s_c;
+      c = found >= 0 ? found : find_contract(L.item_start, L.ncontracts, item);
+    }
     const McContract C = L.contracts[c];
-    const int j = item - __ldg(L.item_start + c);
+    const int base = __ldg(L.item_start + c);
+    const int j = item - base;
     Moments<CV> mo;
     if (METHOD == MC_EUR) {
       eur_item<CV>(C, j, mo);
     } else if (METHOD == MC_ASIA) {
       asia_item<CV>(C, j, mo);
     } else {
-      const int d = C.M;
-      const float* src = L.basket_data + C.basket_off;
-      for (int i = threadIdx.x; i < 2 * d + d * d; i += kBlock) s_fb[i] = src[i];
-      __syncthreads();
+      if (loaded != c) {  // the previous item's readers are past the final barrier
+        const int d = C.M;
+        const float* src = L.basket_data + C.basket_off;
+        for (int i = threadIdx.x; i < 2 * d + d * d; i += kBlock) s_fb[i] = src[i];
+        __syncthreads();
+        loaded = c;
+      }
       basket_item<DMAX, CV>(C, j, s_fb, mo);
-      __syncthreads();
     }
     DF v[kMoments] = {df_of(mo.y), df_of(mo.yy), df_of(mo.g), df_of(mo.gg), df_of(mo.yg)};
     DF tot[kMoments];
     block_sum_df<kMoments>(v, sh, tot);
-    const int base = __ldg(L.item_start + c);
     grid_finalize_df<kMoments>(tot, (float2*)L.partial + (size_t)base * kMoments, L.tickets + c,
                                L.out + (size_t)c * kMoments, C.items, j);
+    if (threadIdx.x == 0) s_c = -1;  // every thread read s_c before block_sum_df's barriers
     __syncthreads();
   }
 }
@@ -353,27 +401,19 @@ __global__ void __launch_bounds__(kBlock) mc_eur_noalloc_kernel(McContract C,
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_addr[kNoAllocMaxDevices];
-int g_noalloc_sms[kNoAllocMaxDevices];
 
 // Per-device set-up, done once with the device current: the device address
-// of the scratch array (host code must not use the symbol itself) and the SM
-// count that sizes the launch.
-int noalloc_setup(int dev, unsigned char** addr, int* sms) {
+// of the scratch array (host code must not use the symbol itself).
+int noalloc_setup(unsigned char** addr, int dev) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_addr[dev]) {
     void* p = nullptr;
-    int st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch),
-                         "cudaGetSymbolAddress(no-alloc scratch)");
+    const int st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch),
+                               "cudaGetSymbolAddress(no-alloc scratch)");
     if (st) return st;
-    int n = 0;
-    st = cuda_status(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev),
-                     "cudaDeviceGetAttribute");
-    if (st) return st;
-    g_noalloc_sms[dev] = n;
     g_noalloc_addr[dev] = (unsigned char*)p;
   }
   *addr = g_noalloc_addr[dev];
-  *sms = g_noalloc_sms[dev];
   return PCF_OK;
 }
 
@@ -399,12 +439,9 @@ extern "C" int pcf_mc_eur_noalloc(double S0, double E, double r, double sigma, d
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return set_error(PCF_EINVAL, "device %d beyond the no-allocation table", dev);
   unsigned char* scratch = nullptr;
-  int sms = 0;
-  st = noalloc_setup(dev, &scratch, &sms);
+  st = noalloc_setup(&scratch, dev);
   if (st) return st;
-  pcf_ctx shape;  // only its SM count is read: it sizes the work items
-  shape.sm_count = sms;
-  const McContract C = make_eur(&shape, S0, E, r, sigma, T, N, payoff_fun, seed, 0);
+  const McContract C = make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0);
   if (C.items > kNoAllocMaxItems)
     return set_error(PCF_EINVAL, "N = %lld needs %d work items; the fixed scratch holds %d", N,
                      C.items, kNoAllocMaxItems);

@@ -188,15 +188,27 @@ static void split_seed(unsigned long long seed, McContract& k) {
   k.seed_hi = (uint32_t)(seed >> 32);
 }
 
-int eur_quads_per_thread(const pcf_ctx* c, long long N) {
+// Work-item sizes depend on the contract alone, so a contract's sums are the
+// same whatever batch, launch or device prices it. An item carries enough
+// path work per thread to amortise its fixed cost (a queue ticket, the
+// contract lookup, a block reduction of five double-float sums and one
+// partial store).
+int eur_quads_per_thread(long long N) {
   const long long nq = (N + 3) / 4;
-  long long per = nq / ((long long)kBlock * c->sm_count * 8);
+  long long per = nq / ((long long)kBlock * 32);  // about 32 items per contract
   per = std::max(1LL, std::min(64LL, per));
   return (int)(per >= 4 ? per & ~3LL : per);  // chunks of 4 quads per Kahan flush
 }
 
-McContract make_eur(const pcf_ctx* c, double S0, double E, double r, double sigma, double T,
-                    long long N, int pf, unsigned long long seed, uint32_t stream) {
+// Asian: at least ~256 monitoring steps per thread per item.
+int asia_paths_per_thread(int M) { return std::max(1, std::min(16, (256 + M - 1) / M)); }
+
+// Basket: a few paths per thread for baskets of up to 8 assets (the kernels
+// for wider baskets take one path per thread).
+int basket_paths_per_thread(int d) { return d <= 4 ? 8 : d <= 8 ? 4 : 1; }
+
+McContract make_eur(double S0, double E, double r, double sigma, double T, long long N, int pf,
+                    unsigned long long seed, uint32_t stream) {
   McContract k;
   memset(&k, 0, sizeof k);
   const double log2e = 1.4426950408889634;
@@ -208,7 +220,7 @@ McContract make_eur(const pcf_ctx* c, double S0, double E, double r, double sigm
   k.l2S0 = (float)(log(S0) * log2e);
   k.nK = (float)(-pf * E);
   k.N = N;
-  k.units_per_item = kBlock * eur_quads_per_thread(c, N);
+  k.units_per_item = kBlock * eur_quads_per_thread(N);
   k.items = (int)(((N + 3) / 4 + k.units_per_item - 1) / k.units_per_item);
   split_seed(seed, k);
   k.stream = stream;
@@ -233,8 +245,8 @@ McContract make_asia(double S0, double E, double r, double sigma, double T, long
   k.M = M;
   k.mode = mode;
   k.N = N;
-  k.units_per_item = kBlock;
-  k.items = (int)((N + kBlock - 1) / kBlock);
+  k.units_per_item = kBlock * asia_paths_per_thread(M);
+  k.items = (int)((N + k.units_per_item - 1) / k.units_per_item);
   split_seed(seed, k);
   k.stream = stream;
   return k;
@@ -271,8 +283,8 @@ int make_basket(int d, const double* S0, const double* sig, const double* corr, 
   k.mode = tri ? 0 : 1;
   k.nK = (float)(-pf * E);
   k.N = N;
-  k.units_per_item = kBlock;
-  k.items = (int)((N + kBlock - 1) / kBlock);
+  k.units_per_item = kBlock * basket_paths_per_thread(d);
+  k.items = (int)((N + k.units_per_item - 1) / k.units_per_item);
   split_seed(seed, k);
   k.stream = stream;
   k.basket_off = (int)fb.size();
@@ -363,7 +375,7 @@ int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double
   if (N > (1LL << 46)) return set_error(PCF_EINVAL, "N must be <= 2^46");
   pcf_ctx* c = resolve_ctx(ctx, &st);
   if (!c) return st;
-  std::vector<McContract> cs{make_eur(c, S0, E, r, sigma, T, N, payoff_fun, seed, 0)};
+  std::vector<McContract> cs{make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0)};
   std::vector<double> sums;
   st = run_mc(c, MC_EUR, cs, {}, 0, false, use_cv != 0, sums);
   if (st) return st;

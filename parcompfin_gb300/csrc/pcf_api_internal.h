@@ -43,8 +43,8 @@ int check_common(double S0, double E, double r, double sigma, double T, long lon
 void fill_result(const double* s, long long n, double mu_g, double disc, bool use_cv,
                  pcf_mc_result* out);
 
-McContract make_eur(const pcf_ctx* c, double S0, double E, double r, double sigma, double T,
-                    long long N, int pf, unsigned long long seed, uint32_t stream);
+McContract make_eur(double S0, double E, double r, double sigma, double T, long long N, int pf,
+                    unsigned long long seed, uint32_t stream);
 McContract make_asia(double S0, double E, double r, double sigma, double T, long long N, int M,
                      int pf, int mode, unsigned long long seed, uint32_t stream);
 double asia_cv_mean(double S0, double E, double r, double sigma, double T, int M, int pf,

@@ -37,7 +37,7 @@ int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContract& k,
   switch (q.method) {
     case PCF_METHOD_EUR:
       if (q.N > (1LL << 46)) return set_error(PCF_EINVAL, "request %d: N too large", idx);
-      k = make_eur(c, q.S0, q.E, q.r, q.sigma, q.T, q.N, q.payoff_fun, q.seed, q.stream);
+      k = make_eur(q.S0, q.E, q.r, q.sigma, q.T, q.N, q.payoff_fun, q.seed, q.stream);
       mu_g = q.S0 * exp(q.r * q.T);
       return PCF_OK;
     case PCF_METHOD_ASIA:
