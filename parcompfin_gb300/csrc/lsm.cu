@@ -104,30 +104,6 @@ __device__ float european_price(const LsmParams& P, float S, float rem) {
   return dK * norm_cdf_f(-d2) - S * norm_cdf_f(-d1);
 }
 
-// include/common.h:98-141: the adjugate over the determinant, then the
-// mat-vec product. The normal matrix of the basis {1, x, x^2} is the symmetric
-// Hankel matrix [[a0,a1,a2],[a1,a2,a3],[a2,a3,a4]], so its adjugate has six
-// distinct cofactors. They are formed with FMAs, and one reciprocal replaces
-// nine divisions. In exact arithmetic this is the reference's solution; FP64
-// is slow on GB300, so the short chain matters (it runs once per date on the
-// critical path).
-__device__ __forceinline__ bool solve3(const double* a, double (&coef)[3]) {
-  const double c00 = fma(a[2], a[4], -a[3] * a[3]);
-  const double c01 = fma(a[2], a[3], -a[1] * a[4]);
-  const double c02 = fma(a[1], a[3], -a[2] * a[2]);
-  const double c11 = fma(a[0], a[4], -a[2] * a[2]);
-  const double c12 = fma(a[1], a[2], -a[0] * a[3]);
-  const double c22 = fma(a[0], a[2], -a[1] * a[1]);
-  const double det = fma(a[0], c00, fma(a[1], c01, a[2] * c02));
-  if (!(det > 0)) return false;
-  const double rd = 1.0 / det;
-  const double y0 = a[5], y1 = a[6], y2 = a[7];
-  coef[0] = fma(c00, y0, fma(c01, y1, c02 * y2)) * rd;
-  coef[1] = fma(c01, y0, fma(c11, y1, c12 * y2)) * rd;
-  coef[2] = fma(c02, y0, fma(c12, y1, c22 * y2)) * rd;
-  return true;
-}
-
 // Dynamic shared memory of one block: two copy mbarriers, the discount and
 // growth tables, per-path state, and two path-slice buffers.
 template <typename TauT>
@@ -168,8 +144,9 @@ struct LsmShared {
   float wpart[kLsmWarps][kRegSums];              // per-warp FP32 sums
   alignas(16) DF xin[2][kMaxCluster][kRegSums];  // cluster: every CTA's totals, by date parity
   alignas(16) DF ctot[kRegSums];                 // this CTA's totals
-  uint64_t xbar[2];                              // cluster: arrivals of the CTAs' totals
-  double t[kRegSums];                            // the contract's sums, FP64
+  uint64_t xbar[2];                              // cluster: bytes of the CTAs' totals
+  DF tdf[kRegSums];                              // the contract's sums, scaled
+  DF cof[8];                                     // adjugate of the normal matrix
   float coef[3];
   int mode;  // 0 skip the date, 1 few in-the-money paths, 2 regression
   int fail;  // a wait gave up
@@ -188,11 +165,17 @@ __device__ __forceinline__ void issue_row(const LsmParams& P, int r, long long p
   bulk_g2s(dst + PB, row + P.Hp + p0, bytes, bar);
 }
 
-// Adds the regression sums of the in-the-money paths of one slice entry.
-__device__ __forceinline__ void reg_accumulate(const LsmParams& P, float Sv, float y, float* acc) {
-  const float x = (Sv - P.E) * P.invE;
+// Adds one path's terms to the regression sums of a date if the path is in
+// the money there (src/mc_amer.cpp:57-66 regresses on in-the-money paths
+// only): x = (S - E)/E and the discounted cash flow y = cfd * growth. Paths
+// out of the money add zeros, so the loop has no divergent branch.
+__device__ __forceinline__ void reg_accumulate(const LsmParams& P, float Sv, float cfd,
+                                               float growth, float (&acc)[kRegSums]) {
+  const bool itm = fmaf(P.pf, Sv, P.nK) > 0.f;
+  const float x = itm ? (Sv - P.E) * P.invE : 0.f;
+  const float y = itm ? cfd * growth : 0.f;
   const float x2 = x * x;
-  acc[0] += 1.f;
+  acc[0] += itm ? 1.f : 0.f;
   acc[1] += x;
   acc[2] += x2;
   acc[3] = fmaf(x2, x, acc[3]);
@@ -269,20 +252,24 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared& X, i
   const int G = P.nblocks;
   DF g{0.f, 0.f};
   if (CLUSTER) {
-    // Every CTA writes its eight totals into xin[slot][b] of every CTA and
-    // arrives on that CTA's xbar[slot]. Slot reuse is safe: a CTA sends date
-    // d-2 only after its wait for date d-1, which needs every peer's date d-1
-    // totals, which each peer sends after reading its date d slot.
+    // Every CTA stores its eight totals into xin[slot][b] of every CTA with
+    // st.async; each store counts its bytes against that CTA's xbar[slot],
+    // which the CTA's own lane 0 arms for G x 64 bytes (a store may land
+    // before the arming: the phase cannot complete before the arming's
+    // arrival). Slot reuse is safe: a CTA sends date d-2 only after its wait
+    // for date d-1, which needs every peer's date d-1 totals, which each peer
+    // sends after it has read its date d slot.
+    if (lane == 0) mbar_arrive_expect_tx(&X.xbar[slot], (uint32_t)(G * kRegSums * sizeof(DF)));
     if (lane < kRegSums) X.ctot[lane] = v;
     __syncwarp();
     if (lane < G) {
       const float4* src = reinterpret_cast<const float4*>(X.ctot);
       const uint32_t dst = cluster_map(&X.xin[slot][b][0], (uint32_t)lane);
+      const uint32_t bar = cluster_map(&X.xbar[slot], (uint32_t)lane);
 #pragma unroll
-      for (int j = 0; j < kRegSums * 2 / 4; ++j) st_cluster_v4(dst + 16u * j, src[j]);
-      mbar_arrive_remote(cluster_map(&X.xbar[slot], (uint32_t)lane));
+      for (int j = 0; j < kRegSums * 2 / 4; ++j) st_async_v4(dst + 16u * j, src[j], bar);
     }
-    if (!mbar_wait_cluster(&X.xbar[slot], (xph >> slot) & 1u, P.copy_wait_limit)) {
+    if (!mbar_wait(&X.xbar[slot], (xph >> slot) & 1u, P.copy_wait_limit)) {
       X.fail = 1;
       atomicExch(P.err, 1);
     }
@@ -306,25 +293,67 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared& X, i
     }
   }
   g = df_add(g, shfl_xor_df(g, 8));
-  g = df_add(g, shfl_xor_df(g, 16));
-  if (lane < kRegSums) X.t[lane] = df_value(g);
+  g = df_add(g, shfl_xor_df(g, 16));  // lanes 0..7: the contract's sum q = lane
+  // include/common.h:98-141 solves the normal equations by the adjugate over
+  // the determinant, then a mat-vec product. The normal matrix of the basis
+  // {1, x, x^2} is the symmetric Hankel matrix [[a0,a1,a2],[a1,a2,a3],
+  // [a2,a3,a4]], so its adjugate has six distinct cofactors:
+  //   c00 = a2 a4 - a3 a3   c01 = a2 a3 - a1 a4   c02 = a1 a3 - a2 a2
+  //   c11 = a0 a4 - a2 a2   c12 = a1 a2 - a0 a3   c22 = a0 a2 - a1 a1
+  // one per lane. Lanes 0..2 then form the numerators adj (a5, a6, a7) and
+  // lane 3 the determinant a0 c00 + a1 c01 + a2 c02, each a three-term dot
+  // product. The arithmetic is double-float (~48 significant bits, enough for
+  // the cancellation in the cofactors) instead of FP64, which is slow on
+  // GB300 and sits on every date's critical path; the sums are first scaled
+  // by a power of two near 1/a0 (exact, and it leaves the solution
+  // unchanged) to keep every product well inside the FP32 exponent range.
+  // The coefficients are used in FP32, so the final division is FP32.
+  const float n = __shfl_sync(0xffffffffu, g.hi, 0);  // in-the-money paths (an exact integer)
+  if (n >= 1.f) {
+    const int e = (__float_as_int(n) >> 23) & 255;  // biased exponent of n, in [127, 254]
+    const float s = __int_as_float((254 - e) << 23);  // 2^-(e - 127), exact
+    g = DF{g.hi * s, g.lo * s};
+  }
+  if (lane < kRegSums) X.tdf[lane] = g;
   __syncwarp();
+  const DF* a = X.tdf;
+  DF cof{0.f, 0.f};
+  if (lane < 6) {
+    const int sh = 4 * lane;  // operand indices of cofactor `lane`, one nibble per lane
+    cof = df_add(df_mul(a[(0x010122 >> sh) & 15], a[(0x224334 >> sh) & 15]),
+                 df_neg(df_mul(a[(0x102213 >> sh) & 15], a[(0x132243 >> sh) & 15])));
+    X.cof[lane] = cof;
+  }
+  __syncwarp();
+  DF dot{0.f, 0.f};
+  if (lane < 4) {
+    const int sh = 4 * lane;  // adjugate row `lane` (row 0 again for lane 3)
+    const DF* y = lane < 3 ? a + 5 : a;
+    dot = df_add(df_add(df_mul(X.cof[(0x0210 >> sh) & 15], y[0]),
+                        df_mul(X.cof[(0x1431 >> sh) & 15], y[1])),
+                 df_mul(X.cof[(0x2542 >> sh) & 15], y[2]));
+  }
+  const DF n1 = shfl_df(dot, 1), n2 = shfl_df(dot, 2), det = shfl_df(dot, 3);
   if (lane == 0) {
-    const double n = X.t[0];
     int mode = 2;
-    double c[3] = {0.0, 0.0, 0.0};
-    if (n == 0.0) {
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    if (n == 0.f) {
       mode = 0;
-    } else if (n <= 2.0) {
+    } else if (n <= 2.f) {
       mode = 1;
-    } else if (!solve3(X.t, c)) {
+    } else if (!(det.hi > 0.f) || !(det.hi < INFINITY)) {  // include/common.h:115-117
       mode = 0;
       if (b == 0) atomicAdd(P.singular, 1);
+    } else {
+      const float r = 1.f / det.hi;
+      c0 = (dot.hi + dot.lo) * r;
+      c1 = (n1.hi + n1.lo) * r;
+      c2 = (n2.hi + n2.lo) * r;
     }
     X.mode = mode;
-    X.coef[0] = (float)c[0];
-    X.coef[1] = (float)c[1];
-    X.coef[2] = (float)c[2];
+    X.coef[0] = c0;
+    X.coef[1] = c1;
+    X.coef[2] = c2;
   }
 }
 
@@ -353,8 +382,8 @@ __device__ void lsm_body(const LsmParams& P, int b) {
     mbar_init(&S.bar[0], 1);
     mbar_init(&S.bar[1], 1);
     if (CLUSTER) {
-      mbar_init(&X.xbar[0], (uint32_t)P.nblocks);
-      mbar_init(&X.xbar[1], (uint32_t)P.nblocks);
+      mbar_init(&X.xbar[0], 1);  // armed by this CTA's lane 0 once per date
+      mbar_init(&X.xbar[1], 1);
     }
     fence_mbar_init();
     X.fail = 0;
@@ -363,20 +392,28 @@ __device__ void lsm_body(const LsmParams& P, int b) {
   // ---- forward: generate and store paths ----
   const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
   const float dM = P.dtab[M];
+  const size_t stride = (size_t)2 * P.Hp;  // floats per row
+  const float nb2 = -P.b2;
+#pragma unroll 2
   for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
     const long long p = p0 + i;
     float Lp = 0.f, Lm = 0.f, Sp = 0.f, Sm = 0.f;
-    float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int m = 1; m <= M; ++m) {
-      if (((m - 1) & 3) == 0) z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)((m - 1) >> 2)));
-      const float z = lane4(z4, (m - 1) & 3);
-      Lp += fmaf(P.b2, z, P.a2);
-      Lm += fmaf(-P.b2, z, P.a2);
-      Sp = ex2_approx(P.l2S0 + Lp);
-      Sm = ex2_approx(P.l2S0 + Lm);
-      float* row = P.paths + (size_t)(m - 1) * 2 * P.Hp;
-      row[p] = Sp;
-      row[P.Hp + p] = Sm;
+    float* row = P.paths + p;
+    for (int m0 = 0; m0 < M; m0 += 4) {
+      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(m0 >> 2)));
+      const float zz[4] = {z4.x, z4.y, z4.z, z4.w};
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        if (m0 + l < M) {  // date m0 + l + 1 takes lane l
+          Lp += fmaf(P.b2, zz[l], P.a2);
+          Lm += fmaf(nb2, zz[l], P.a2);
+          Sp = ex2_approx(P.l2S0 + Lp);
+          Sm = ex2_approx(P.l2S0 + Lm);
+          row[0] = Sp;
+          row[P.Hp] = Sm;
+          row += stride;
+        }
+      }
     }
     S.cf[i] = lsm_payoff(P, Sp) * dM;
     S.cf[PB + i] = lsm_payoff(P, Sm) * dM;
@@ -437,8 +474,7 @@ __device__ void lsm_body(const LsmParams& P, int b) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + i;
-        const float Sv = sl[s];
-        if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * e1, acc);
+        reg_accumulate(P, sl[s], S.cf[s], e1, acc);
       }
     }
     regress(acc, M - 1, -1, 0);
@@ -458,34 +494,32 @@ __device__ void lsm_body(const LsmParams& P, int b) {
     float acc[kRegSums];
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
+#pragma unroll 2
     for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + i;
+        float cfd = S.cf[s];
         // Exercise decision at date m (src/mc_amer.cpp:73-106).
         if (mode != 0) {
           const float Sv = cur[s];
-          const float pv = lsm_payoff(P, Sv);
-          if (pv > 0.f) {
-            float cont, ex = pv;
-            if (mode == 1) {
-              cont = S.cf[s] * em;
-            } else {
-              const float x = (Sv - P.E) * P.invE;
-              cont = fmaf(fmaf(c2, x, c1), x, c0);
-              // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E).
-              if (P.ref_exercise) ex = fmaxf(P.pf * (Sv - 2.f * P.E), 0.f);
-            }
-            if (ex > cont) {
-              S.cf[s] = ex * dm;
-              S.tau[s] = (TauT)m;
-            }
+          const float v = fmaf(P.pf, Sv, P.nK);  // the payoff before its max with 0
+          float cont, ex = v;
+          if (mode == 1) {
+            cont = cfd * em;
+          } else {
+            const float x = (Sv - P.E) * P.invE;
+            cont = fmaf(fmaf(c2, x, c1), x, c0);
+            // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E).
+            if (P.ref_exercise) ex = fmaxf(P.pf * (Sv - 2.f * P.E), 0.f);
+          }
+          if (v > 0.f && ex > cont) {
+            cfd = ex * dm;
+            S.cf[s] = cfd;
+            S.tau[s] = (TauT)m;
           }
         }
-        if (has_next) {
-          const float Sv = nxt[s];
-          if (lsm_payoff(P, Sv) > 0.f) reg_accumulate(P, Sv, S.cf[s] * e1, acc);
-        }
+        if (has_next) reg_accumulate(P, nxt[s], cfd, e1, acc);
       }
     }
     if (!has_next) break;

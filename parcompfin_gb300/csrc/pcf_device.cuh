@@ -134,6 +134,24 @@ __device__ __forceinline__ DF df_add_f(DF a, float b) {  // df_add(a, {b, 0})
   return DF{hi, e - (hi - s)};
 }
 
+// Double-float product: the FP32 product of the high parts, its exact
+// rounding error (an FMA) plus the cross terms, renormalised. The explicit
+// _rn operations keep the compiler from contracting them into FMAs.
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float hi = __fadd_rn(p, e);
+  return DF{hi, __fsub_rn(e, __fsub_rn(hi, p))};
+}
+
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+
+__device__ __forceinline__ DF shfl_df(DF v, int src) {
+  return DF{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
 __device__ __forceinline__ DF shfl_xor_df(DF v, int o) {
   return DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
 }
@@ -333,34 +351,16 @@ __device__ __forceinline__ uint32_t cluster_map(const void* p, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_cluster_v4(uint32_t addr, float4 v) {
-  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x),
-               "f"(v.y), "f"(v.z), "f"(v.w)
-               : "memory");
-}
-// Arrives on an mbarrier of another CTA of the cluster; releases this
-// thread's earlier shared::cluster stores to whoever completes the wait.
-__device__ __forceinline__ void mbar_arrive_remote(uint32_t bar_cluster_addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(
-                   bar_cluster_addr)
-               : "memory");
-}
-// mbar_wait with cluster-scope acquire: the waiting thread sees what the
-// arriving threads of other CTAs stored before their arrive. Bounded.
-__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity,
-                                                  uint32_t limit) {
-  for (uint32_t i = 0; i < limit; ++i) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
+// Asynchronous store of 16 bytes into another CTA's shared memory; its
+// completion counts 16 bytes against that CTA's mbarrier (complete_tx), so
+// the sender needs no fence and the receiver sees the data once the phase
+// completes.
+__device__ __forceinline__ void st_async_v4(uint32_t addr, float4 v, uint32_t bar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, "
+      "[%5];" ::"r"(addr),
+      "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(bar)
+      : "memory");
 }
 
 // Group barrier for a persistent kernel whose blocks are co-resident (the
