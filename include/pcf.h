@@ -212,8 +212,15 @@ typedef struct pcf_mc_request {
  * traffic. */
 typedef struct pcf_plan pcf_plan;
 PCF_API int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** out);
-/* Enqueue the plan's kernels on the context stream; returns without waiting. */
+/* Enqueue the plan's kernels on the context stream; returns without waiting.
+ * From the second launch on, the launch sequence is captured once in a CUDA
+ * graph and replayed (falling back to direct launches if capture fails). */
 PCF_API int pcf_plan_launch(pcf_plan* plan);
+/* mode 1 (default): replay through a CUDA graph from the second launch;
+ * mode 0: always launch directly (drops a captured graph). */
+PCF_API int pcf_plan_set_graph(pcf_plan* plan, int mode);
+/* 1 if the plan's launches now replay a CUDA graph. */
+PCF_API int pcf_plan_uses_graph(const pcf_plan* plan);
 /* Wait for the plan's last launch and fill results[n]. */
 PCF_API int pcf_plan_results(pcf_plan* plan, pcf_mc_result* results);
 /* Kernels one pcf_plan_launch enqueues. */

@@ -136,6 +136,8 @@ SIGNATURES = {
     "pcf_binom_embar_batch": (_I, [_P, _I, C.POINTER(BinomContract), _I, _PD]),
     "pcf_plan_create": (_I, [_P, _I, C.POINTER(McRequest), C.POINTER(_P)]),
     "pcf_plan_launch": (_I, [_P]),
+    "pcf_plan_set_graph": (_I, [_P, _I]),
+    "pcf_plan_uses_graph": (_I, [_P]),
     "pcf_plan_results": (_I, [_P, C.POINTER(McResult)]),
     "pcf_plan_kernel_count": (_I, [_P]),
     "pcf_plan_destroy": (_I, [_P]),

@@ -203,14 +203,22 @@ def _pack(reqs):
 
 
 class Plan:
-    """Device-resident batch: upload once, launch many times (graph-capturable)."""
+    """Device-resident batch: upload once, launch many times. From the second
+    launch on the launch sequence replays a CUDA graph (graph=False: always
+    launch directly)."""
 
-    def __init__(self, reqs, ctx=None):
+    def __init__(self, reqs, ctx=None, graph=True):
         lib = _lib.load()
         arr, keep = _pack(reqs)
         h = C.c_void_p()
         _lib.check(lib.pcf_plan_create(_h(ctx), len(reqs), arr, C.byref(h)))
         self._h, self.n = h, len(reqs)
+        if not graph:
+            _lib.check(lib.pcf_plan_set_graph(self._h, 0))
+
+    @property
+    def uses_graph(self) -> bool:
+        return bool(_lib.load().pcf_plan_uses_graph(self._h))
 
     def launch(self):
         _lib.check(_lib.load().pcf_plan_launch(self._h))

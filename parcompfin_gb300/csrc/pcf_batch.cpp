@@ -284,7 +284,9 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
   return PCF_OK;
 }
 
-int plan_launch(pcf_plan* p) {
+// The plan's launch sequence: ticket reset, one persistent launch per Monte
+// Carlo group, the LSM launches.
+int plan_enqueue(pcf_plan* p) {
   pcf_ctx* c = p->ctx;
   if (p->tickets_bytes) {
     int st = cuda_status(cudaMemsetAsync(p->d_tickets, 0, p->tickets_bytes, p->stream),
@@ -299,6 +301,46 @@ int plan_launch(pcf_plan* p) {
   }
   if (p->lsm) return lsm_batch_launch(c, p->lsm, p->stream);
   return PCF_OK;
+}
+
+// Captures the launch sequence into a CUDA graph (every address in it is
+// fixed for the plan's life). Returns false, leaving the stream out of
+// capture, if the capture or the instantiation fails.
+bool plan_capture(pcf_plan* p) {
+  pcf_ctx* c = p->ctx;
+  if (cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const long long before = c->launches;
+  const int st = plan_enqueue(p);
+  p->graph_kernels = c->launches - before;
+  c->launches = before;
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+  bool ok = st == PCF_OK && e == cudaSuccess && g != nullptr;
+  if (ok) ok = cudaGraphInstantiate(&p->gexec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    p->gexec = nullptr;
+    cudaGetLastError();
+  }
+  return ok;
+}
+
+int plan_launch(pcf_plan* p) {
+  pcf_ctx* c = p->ctx;
+  if (!p->gexec && p->graph_mode && !p->graph_failed && p->launches_done >= 1)
+    p->graph_failed = !plan_capture(p);
+  int st;
+  if (p->gexec) {
+    st = cuda_status(cudaGraphLaunch(p->gexec, p->stream), "plan graph launch");
+    if (!st) c->launches += p->graph_kernels;
+  } else {
+    st = plan_enqueue(p);
+  }
+  if (!st) p->launches_done += 1;
+  return st;
 }
 
 int plan_fetch(pcf_plan* p) {
@@ -355,6 +397,20 @@ int pcf_plan_launch(pcf_plan* p) {
   return plan_launch(p);
 }
 
+int pcf_plan_set_graph(pcf_plan* p, int mode) {
+  if (!p || mode < 0 || mode > 1) return set_error(PCF_EINVAL, "bad arguments");
+  cudaSetDevice(p->ctx->device);
+  p->graph_mode = mode;
+  if (!mode && p->gexec) {
+    cudaStreamSynchronize(p->stream);
+    cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+  }
+  return PCF_OK;
+}
+
+int pcf_plan_uses_graph(const pcf_plan* p) { return p && p->gexec ? 1 : 0; }
+
 int pcf_plan_kernel_count(const pcf_plan* p) {
   return p ? (int)p->groups.size() + (p->lsm ? lsm_batch_kernels(p->lsm) : 0) : 0;
 }
@@ -372,6 +428,7 @@ int pcf_plan_destroy(pcf_plan* p) {
   if (!p) return PCF_OK;
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->stream);
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
   lsm_batch_destroy(p->lsm);
   if (p->d_mem) cudaFree(p->d_mem);
   if (p->h_own) cudaFreeHost(p->h_own);

@@ -42,6 +42,13 @@ struct pcf_plan {
   std::vector<pcf_mc_request> amer_q;  // their parameters (for the estimators)
   int* d_amer_flags = nullptr;
   int* h_amer_flags = nullptr;
+  // CUDA graph replay: the second launch captures the launch sequence, later
+  // launches replay it. graph_mode 0 never captures.
+  int graph_mode = 1;
+  long long launches_done = 0;
+  bool graph_failed = false;
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_kernels = 0;
 };
 
 namespace pcf {

@@ -102,3 +102,47 @@ def test_batch_rejects_bad_requests(ctx):
         pcf.price_batch([pcf.request("amer", 100, 100, .05, .3, 1.0, 1001, "put", M=50)], ctx=ctx)
     with pytest.raises(ValueError):
         pcf.price_batch([pcf.request("asia", 100, 100, .05, .3, 1.0, 1000, "put", M=0)], ctx=ctx)
+
+
+def test_plan_graph_replay_matches_direct_launches(ctx):
+    """From its second launch a plan replays a CUDA graph of its launch
+    sequence; the sums are the same bits as direct launches."""
+    import parcompfin_gb300 as pcf
+    reqs = _mixed(pcf)
+    with pcf.Plan(reqs, ctx=ctx, graph=False) as direct:
+        for _ in range(2):
+            direct.launch()
+        a = direct.results()
+        assert not direct.uses_graph
+    with pcf.Plan(reqs, ctx=ctx) as plan:
+        plan.launch()
+        first = plan.results()
+        assert not plan.uses_graph
+        before = ctx.launches
+        for _ in range(3):
+            plan.launch()
+        again = plan.results()
+        assert plan.uses_graph
+        assert ctx.launches - before == 3 * plan.kernel_count
+    for x, y, z in zip(a, first, again):
+        assert list(x.sums) == list(y.sums) == list(z.sums)
+
+
+def test_plan_graph_with_a_cooperative_contract(orc, ctx):
+    """An American contract too large for one cluster runs the cooperative
+    kernel; its plan replays the same sums whether or not the capture of a
+    cooperative launch is supported."""
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("amer", 100, 100, .05, .3, 1.0, 1 << 19, "put", M=50, seed=5, stream=0),
+            pcf.request("eur", 100, 95, .05, .2, 1.0, 100_000, "call", seed=1, stream=1)]
+    with pcf.Plan(reqs, ctx=ctx) as plan:
+        plan.launch()
+        first = plan.results()
+        for _ in range(2):
+            plan.launch()
+        again = plan.results()
+    for x, y in zip(first, again):
+        assert list(x.sums) == list(y.sums)
+    s = (C.c_double * 6)()
+    orc.twin_mc_amer(100, 100, .05, .3, 1.0, 1 << 19, 50, -1, 0, 5, 0, s)
+    assert abs(again[0].sums[0] - s[0]) <= 3e-4 * abs(s[0])
