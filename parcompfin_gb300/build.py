@@ -48,7 +48,7 @@ def _sources():
 
 
 def _stale() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return True
     t = os.path.getmtime(LIB)
     for name in os.listdir(CSRC):
@@ -88,7 +88,39 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
+
+
+# The drop-in command-line programs: one executable (pcf_cli.cpp) linked
+# against libpcf.so, reachable under every reference program name in _lib/bin.
+CLI = os.path.join(OUT_DIR, "pcf_cli")
+CLI_BIN = os.path.join(OUT_DIR, "bin")
+CLI_NAMES = [m + v for m in ("mc_eur", "mc_eur_multi", "mc_asia", "mc_amer", "binom_embar")
+             for v in ("", "_omp", "_mpi", "_hybrid")]
+
+
+def build_cli() -> str:
+    src = os.path.join(CSRC, "pcf_cli.cpp")
+    if not os.path.exists(src):
+        return ""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("a C++ compiler is required to build pcf_cli")
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", src, "-o", tmp, "-L" + OUT_DIR, "-lpcf",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"pcf_cli build failed:\n{r.stderr}")
+    os.replace(tmp, CLI)
+    os.makedirs(CLI_BIN, exist_ok=True)
+    for name in CLI_NAMES:
+        link = os.path.join(CLI_BIN, name)
+        if os.path.lexists(link):
+            os.remove(link)
+        os.symlink(os.path.join("..", "pcf_cli"), link)
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,0 +1,58 @@
+"""The drop-in command-line programs (parcompfin_gb300/csrc/pcf_cli.cpp), on
+the CPU: every reference program name exists, argv errors fail like the
+reference's programs (no GPU needed for these)."""
+import os
+import subprocess
+
+import pytest
+
+from parcompfin_gb300 import build as B
+
+
+@pytest.fixture(scope="module")
+def bindir():
+    B.build()
+    return B.CLI_BIN
+
+
+def run(path, *args, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([path, *map(str, args)], capture_output=True, text=True, env=e,
+                          timeout=120)
+
+
+def test_every_reference_program_name_is_installed(bindir):
+    for stem in ("mc_eur", "mc_eur_multi", "mc_asia", "mc_amer", "binom_embar"):
+        for v in ("", "_omp", "_mpi", "_hybrid"):
+            p = os.path.join(bindir, stem + v)
+            assert os.path.islink(p) and os.access(p, os.X_OK), p
+
+
+def test_unknown_payoff_is_an_error(bindir):
+    # src/mc_eur.cpp:40 throws std::invalid_argument("Unknown payoff function").
+    r = run(os.path.join(bindir, "mc_eur"), "straddle", 100, 100, .05, .2, 1, 1000)
+    assert r.returncode == 1 and "Unknown payoff function" in r.stderr
+
+
+def test_missing_arguments_print_usage(bindir):
+    r = run(os.path.join(bindir, "mc_asia"), "call", 100, 100, .05, .2, 1, 1000)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = run(os.path.join(bindir, "mc_eur_omp"), "call", 100, 100, .05, .2, 1, 1000)
+    assert r.returncode == 2  # the OpenMP program takes a thread count
+    r = run(B.CLI)
+    assert r.returncode == 2
+
+
+def test_bad_number_is_an_error(bindir):
+    r = run(os.path.join(bindir, "binom_embar"), "put", "abc", 100, .05, .2, 1, 1000)
+    assert r.returncode == 1
+
+
+def test_first_argument_selects_the_program(bindir):
+    r = run(B.CLI, "mc_amer", "call", 100, 100, .05, .2, 1, 1000, 10, env={"PCF_DEVICE": "0"})
+    # Either a GPU priced it (16 columns) or there is none and it says so.
+    if r.returncode == 0:
+        assert len(r.stdout.strip().split(",")) == 16
+    else:
+        assert r.returncode == 1 and r.stderr.strip()

@@ -1,0 +1,86 @@
+"""The drop-in command-line programs on the GPU: the reference's argv in,
+its 16-column CSV line out (include/common.h:212-249), the same prices as the
+C ABI for the same seed, and binom_embar within 1e-10 of the reference."""
+import math
+import os
+import subprocess
+
+import pytest
+
+from parcompfin_gb300 import build as B
+
+pytestmark = pytest.mark.gpu
+
+COLS = ["Method", "Payoff", "S0", "E", "r", "sigma", "T", "N", "M", "Parallel",
+        "Nr_of_assets", "T_overall", "T_calculation", "Result", "Abs_Error", "Error"]
+
+
+def run(name, *args, cwd=None, **env):
+    B.build()
+    e = dict(os.environ)
+    e.update({"PCF_SEED": "7", "PCF_FULL_PRECISION": "1"})
+    e.update({k: str(v) for k, v in env.items()})
+    r = subprocess.run([os.path.join(B.CLI_BIN, name), *map(str, args)], capture_output=True,
+                       text=True, env=e, cwd=cwd, timeout=300)
+    assert r.returncode == 0, r.stderr
+    row = r.stdout.strip().split(",")
+    assert len(row) == 16, r.stdout
+    return dict(zip(COLS, row))
+
+
+def test_mc_eur_columns_and_price():
+    import parcompfin_gb300 as pcf
+    row = run("mc_eur", "call", 100, 100, 0.05, 0.2, 1, 1000000, PCF_COMPARISON=10.450583572185565)
+    assert row["Method"] == "Serial" and row["Payoff"] == "call"
+    assert [row[k] for k in ("S0", "E", "r", "sigma", "T", "N", "M", "Parallel", "Nr_of_assets")] \
+        == ["100", "100", "0.05", "0.2", "1", "1000000", "0", "0", "1"]
+    res = pcf.mc_eur_result(100, 100, .05, .2, 1.0, 1000000, "call", seed=7)
+    assert float(row["Result"]) == res.price_plain
+    assert float(row["Error"]) == res.price_plain - 10.450583572185565
+    assert float(row["Abs_Error"]) == abs(res.price_plain - 10.450583572185565)
+    assert abs(float(row["Error"])) < 4 * res.std_error_plain
+    assert 0 <= float(row["T_calculation"]) <= float(row["T_overall"])
+
+
+def test_variant_labels_and_parallel_column():
+    assert run("mc_eur_omp", "put", 100, 110, .02, .75, 1, 100000, 16)["Method"] == "OMP"
+    assert run("mc_eur_omp", "put", 100, 110, .02, .75, 1, 100000, 16)["Parallel"] == "16"
+    assert run("mc_eur_mpi", "put", 100, 110, .02, .75, 1, 100000)["Parallel"] == "1"
+    assert run("mc_eur_hybrid", "put", 100, 110, .02, .75, 1, 100000, 8)["Parallel"] == "1008"
+
+
+def test_comparison_from_the_reference_header(tmp_path):
+    # The reference's run scripts write include/comparison.h before each sweep.
+    (tmp_path / "include").mkdir()
+    (tmp_path / "include" / "comparison.h").write_text("#pragma once\ndouble comparison = 9.5;\n")
+    row = run("binom_embar", "call", 100, 100, .05, .2, 1, 1000, cwd=tmp_path)
+    assert float(row["Error"]) == pytest.approx(float(row["Result"]) - 9.5, abs=1e-12)
+
+
+def test_asia_amer_multi_match_the_c_abi():
+    import parcompfin_gb300 as pcf
+    row = run("mc_asia", "call", 100, 100, .04, .3, 1.5, 40000, 52)
+    assert row["M"] == "52"
+    assert float(row["Result"]) == pcf.mc_asia_result(100, 100, .04, .3, 1.5, 40000, 52, "call",
+                                                      seed=7).price_plain
+    row = run("mc_amer", "put", 100, 100, .05, .3, 1, 20000, 50)
+    assert row["M"] == "50"
+    assert float(row["Result"]) == pcf.mc_amer_result(100, 100, .05, .3, 1.0, 20000, 50, "put",
+                                                      seed=7).price_plain
+    row = run("mc_eur_multi", "call", 100, 100, .1, .2, 1, 200000, 4, .5)
+    assert row["Nr_of_assets"] == "4" and row["M"] == "0"
+    assert float(row["Result"]) == pcf.mc_eur_multi_result(100, 100, .1, .2, 1.0, 200000, "call",
+                                                           4, .5, seed=7).price_plain
+
+
+def test_binom_embar_matches_the_reference(orc):
+    row = run("binom_embar", "put", 100, 90, .03, .4, .5, 999)
+    ref = orc.ref_binom_embar(100, 90, .03, .4, .5, 999, -1.0)
+    assert abs(float(row["Result"]) - ref) <= 1e-10 * abs(ref)
+
+
+def test_amer_odd_paths_fail_like_the_reference():
+    B.build()
+    r = subprocess.run([os.path.join(B.CLI_BIN, "mc_amer"), "put", "100", "100", ".05", ".3", "1",
+                        "1001", "50"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1 and "divisible by 2" in r.stderr
