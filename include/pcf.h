@@ -152,6 +152,14 @@ PCF_API int pcf_binom_embar(pcf_ctx* ctx, double S0, double E, double r, double 
 PCF_API int pcf_binom_embar_batch(pcf_ctx* ctx, int n, const pcf_binom_contract* contracts,
                                   int mode, double* prices);
 
+/* European or American option by backward induction on the same lattice.
+ * Replaces double binom(S0,E,r,sigma,T,N,payoff_fun) of
+ * src/binom_vanilla_eur.cpp:5-39 (american = 0) and
+ * src/binom_vanilla_amer.cpp:5-40 (american = 1): bit for bit the reference's
+ * FP64 result. One cooperative launch; 1 <= N <= 2,000,000. */
+PCF_API int pcf_binom_vanilla(pcf_ctx* ctx, double S0, double E, double r, double sigma,
+                              double T, int N, int payoff_fun, int american, double* price);
+
 /* European option, single-step GBM Monte Carlo, with no memory allocation.
  * Has no counterpart in the reference: it serves callers that cannot call
  * cudaMalloc while pricing, such as a plugin hosted by a framework whose

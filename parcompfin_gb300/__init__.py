@@ -9,6 +9,8 @@ from .api import (  # noqa: F401
     Plan,
     binom_embar,
     binom_embar_batch,
+    binom_vanilla_amer,
+    binom_vanilla_eur,
     price_batch,
     serve_trace,
     request,

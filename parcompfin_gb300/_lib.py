@@ -134,6 +134,7 @@ SIGNATURES = {
     "pcf_mc_eur_noalloc": (_I, [_D, _D, _D, _D, _D, _LL, _I, _ULL, _P, _P]),
     "pcf_binom_embar": (_I, [_P, _D, _D, _D, _D, _D, _I, _I, _I, _PD]),
     "pcf_binom_embar_batch": (_I, [_P, _I, C.POINTER(BinomContract), _I, _PD]),
+    "pcf_binom_vanilla": (_I, [_P, _D, _D, _D, _D, _D, _I, _I, _I, _PD]),
     "pcf_plan_create": (_I, [_P, _I, C.POINTER(McRequest), C.POINTER(_P)]),
     "pcf_plan_launch": (_I, [_P]),
     "pcf_plan_set_graph": (_I, [_P, _I]),

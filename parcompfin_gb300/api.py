@@ -10,6 +10,9 @@ does:
     mc_asia(S0, E, r, sigma, T, N, M, payoff_fun)        src/mc_asia.cpp:5-40
     mc_amer(S0, E, r, sigma, T, N, M, payoff_fun)        src/mc_amer.cpp:5-114
     binom_embar(S0, E, r, sigma, T, N, payoff_fun)       src/binom_embar.cpp:5-50
+    binom_vanilla_eur(S0, E, r, sigma, T, N, payoff_fun) src/binom_vanilla_eur.cpp:5-39
+    binom_vanilla_amer(S0, E, r, sigma, T, N, payoff_fun)
+                                                          src/binom_vanilla_amer.cpp:5-40
 
 payoff_fun is +1/-1 (the reference's encoding, include/common.h:56-60) or
 the strings "call"/"put" its command lines accept (src/mc_eur.cpp:39-42).
@@ -165,6 +168,26 @@ def binom_embar_batch(contracts, *, mode="reference", ctx=None) -> list:
     out = (C.c_double * len(cs))()
     _lib.check(lib.pcf_binom_embar_batch(_h(ctx), len(cs), arr, BINOM_MODES.get(mode, mode), out))
     return list(out)
+
+
+def _binom_vanilla(S0, E, r, sigma, T, N, payoff_fun, american, ctx):
+    lib = _lib.load()
+    out = C.c_double()
+    _lib.check(lib.pcf_binom_vanilla(_h(ctx), S0, E, r, sigma, T, int(N), payoff_code(payoff_fun),
+                                     1 if american else 0, C.byref(out)))
+    return out.value
+
+
+def binom_vanilla_eur(S0, E, r, sigma, T, N, payoff_fun, *, ctx=None) -> float:
+    """src/binom_vanilla_eur.cpp:5-39 (function binom): European backward
+    induction on the reference's lattice, bit for bit its FP64 result."""
+    return _binom_vanilla(S0, E, r, sigma, T, N, payoff_fun, False, ctx)
+
+
+def binom_vanilla_amer(S0, E, r, sigma, T, N, payoff_fun, *, ctx=None) -> float:
+    """src/binom_vanilla_amer.cpp:5-40 (function binom): American backward
+    induction on the reference's lattice, bit for bit its FP64 result."""
+    return _binom_vanilla(S0, E, r, sigma, T, N, payoff_fun, True, ctx)
 
 
 METHODS = {"eur": _lib.METHOD_EUR, "asia": _lib.METHOD_ASIA, "basket": _lib.METHOD_BASKET,

@@ -23,12 +23,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "-Xcompiler", "-fvisibility=hidden"]
 
-# (source, extra flags). The binomial unit must not contract a*b+c into FMA:
-# it reproduces the reference's FP64 rounding sequence term by term.
+# (source, extra flags). The binomial and lattice units must not contract
+# a*b+c into FMA: they reproduce the reference's FP64 rounding term by term.
 SOURCES = [
     ("mc_kernels.cu", []),
     ("lsm.cu", []),
     ("binom.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("lattice.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("pcf_api.cpp", []),
     ("pcf_batch.cpp", []),
     ("pcf_server.cpp", []),
@@ -97,7 +98,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 CLI = os.path.join(OUT_DIR, "pcf_cli")
 CLI_BIN = os.path.join(OUT_DIR, "bin")
 CLI_NAMES = [m + v for m in ("mc_eur", "mc_eur_multi", "mc_asia", "mc_amer", "binom_embar")
-             for v in ("", "_omp", "_mpi", "_hybrid")]
+             for v in ("", "_omp", "_mpi", "_hybrid")] + ["binom_vanilla_eur", "binom_vanilla_amer"]
 
 
 def build_cli() -> str:

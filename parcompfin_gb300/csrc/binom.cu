@@ -46,6 +46,20 @@
 
 namespace pcf {
 
+// The reference's lattice parameters, src/binom_embar.cpp:19-27 and
+// src/binom_vanilla_eur.cpp:14-22 (this unit's host code is compiled with
+// -ffp-contract=off, like the reference on x86-64).
+void lattice(double r, double sigma, double T, int N, double& u, double& d, double& p,
+             double& q, double& R) {
+  const double dt = (double)T / (double)N;
+  const double beta = 0.5 * (exp(-r * dt) + exp((r + pow(sigma, 2)) * dt));
+  u = beta + sqrt(pow(beta, 2) - 1);
+  d = beta - sqrt(pow(beta, 2) - 1);
+  R = exp(r * dt);
+  p = (R - d) / (u - d);
+  q = 1 - p;
+}
+
 namespace {
 
 constexpr int kEmin = -1;  // binades of the comb() accumulator with integer tables
@@ -291,19 +305,6 @@ __global__ void __launch_bounds__(kBinomBlock) binom_kernel(BinomLaunch L) {
 }
 
 // ---- host side ----
-
-// The reference's lattice parameters, src/binom_embar.cpp:19-27 (this unit's
-// host code is compiled with -ffp-contract=off, like the reference on x86-64).
-void lattice(double r, double sigma, double T, int N, double& u, double& d, double& p,
-             double& q, double& R) {
-  const double dt = (double)T / (double)N;
-  const double beta = 0.5 * (exp(-r * dt) + exp((r + pow(sigma, 2)) * dt));
-  u = beta + sqrt(pow(beta, 2) - 1);
-  d = beta - sqrt(pow(beta, 2) - 1);
-  R = exp(r * dt);
-  p = (R - d) / (u - d);
-  q = 1 - p;
-}
 
 struct HostTables {
   std::vector<double> logt;

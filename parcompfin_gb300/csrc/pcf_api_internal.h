@@ -53,6 +53,10 @@ int make_basket(int d, const double* S0, const double* sig, const double* corr, 
                 double T, double E, long long N, int pf, double ts, unsigned long long seed,
                 uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g);
 
+// The reference's beta-parametrised lattice (binom.cu).
+void lattice(double r, double sigma, double T, int N, double& u, double& d, double& p,
+             double& q, double& R);
+
 // American (Longstaff-Schwartz) contracts in a batch (lsm.cu).
 struct LsmRequest {
   double S0, E, r, sigma, T;

@@ -16,6 +16,7 @@
 //   mc_asia[_omp|_mpi|_hybrid]       payoff S0 E r sigma T N M [threads]
 //   mc_amer[_omp|_mpi|_hybrid]       payoff S0 E r sigma T N M [threads]
 //   binom_embar[_omp|_mpi|_hybrid]   payoff S0 E r sigma T N [threads]
+//   binom_vanilla_eur, binom_vanilla_amer   payoff S0 E r sigma T N
 // The threads argument is accepted and reported in the Parallel column, as
 // the reference's OpenMP (threads), MPI (ranks: 1 here) and hybrid
 // (ranks*1000 + threads) programs report it.
@@ -143,7 +144,8 @@ int usage() {
           "  mc_eur_multi[_omp|_mpi|_hybrid] payoff S0 E r sigma T N assets rho [threads]\n"
           "  mc_asia[_omp|_mpi|_hybrid]      payoff S0 E r sigma T N M [threads]\n"
           "  mc_amer[_omp|_mpi|_hybrid]      payoff S0 E r sigma T N M [threads]\n"
-          "  binom_embar[_omp|_mpi|_hybrid]  payoff S0 E r sigma T N [threads]\n");
+          "  binom_embar[_omp|_mpi|_hybrid]  payoff S0 E r sigma T N [threads]\n"
+          "  binom_vanilla_eur, binom_vanilla_amer  payoff S0 E r sigma T N\n");
   return 2;
 }
 
@@ -161,7 +163,8 @@ int main(int argc, char** argv) {
   }
   std::string stem = prog;
   Variant var{"Serial", 0};
-  if (ends_with(prog, "_omp", &stem)) var = Variant{"OMP", 1};
+  if (prog == "binom_vanilla_eur" || prog == "binom_vanilla_amer") var = Variant{"Serial_vanilla", 0};
+  else if (ends_with(prog, "_omp", &stem)) var = Variant{"OMP", 1};
   else if (ends_with(prog, "_mpi", &stem)) var = Variant{"MPI", 0};
   else if (ends_with(prog, "_hybrid", &stem)) var = Variant{"Hybrid", 1};
   char** av = argv + a0;
@@ -170,7 +173,7 @@ int main(int argc, char** argv) {
   const int nbase = stem == "mc_eur_multi" ? 10 : (stem == "mc_asia" || stem == "mc_amer") ? 9
                                                                                              : 8;
   if (stem != "mc_eur" && stem != "mc_eur_multi" && stem != "mc_asia" && stem != "mc_amer" &&
-      stem != "binom_embar")
+      stem != "binom_embar" && stem != "binom_vanilla_eur" && stem != "binom_vanilla_amer")
     return usage();
   if (ac < nbase + var.threads_arg) return usage();
   const char* payoff = av[1];
@@ -224,9 +227,12 @@ int main(int argc, char** argv) {
   } else if (stem == "mc_amer") {
     st = pcf_mc_amer(ctx, S0, E, r, sigma, T, N, (int)M, pf, env_flag("PCF_REF_EXERCISE"), seed,
                      cv, &res);
-  } else {
+  } else if (stem == "binom_embar") {
     st = pcf_binom_embar(ctx, S0, E, r, sigma, T, (int)N, pf, env_flag("PCF_BINOM_MODE"),
                          &result);
+  } else {
+    st = pcf_binom_vanilla(ctx, S0, E, r, sigma, T, (int)N, pf, stem == "binom_vanilla_amer",
+                           &result);
   }
   const Clock::time_point end = Clock::now();
   if (st) {
@@ -234,7 +240,7 @@ int main(int argc, char** argv) {
     pcf_ctx_destroy(ctx);
     return 1;
   }
-  if (stem != "binom_embar") result = cv ? res.price_cv : res.price_plain;
+  if (stem.compare(0, 5, "binom") != 0) result = cv ? res.price_cv : res.price_plain;
   const double t_calc = std::chrono::duration<double>(end - start).count();
   const double t_overall = std::chrono::duration<double>(end - start_overall).count();
   const int m_col = (stem == "mc_asia" || stem == "mc_amer") ? (int)M : 0;

@@ -84,3 +84,11 @@ def test_amer_odd_paths_fail_like_the_reference():
     r = subprocess.run([os.path.join(B.CLI_BIN, "mc_amer"), "put", "100", "100", ".05", ".3", "1",
                         "1001", "50"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 1 and "divisible by 2" in r.stderr
+
+
+def test_vanilla_lattice_programs(orc):
+    row = run("binom_vanilla_amer", "put", 100, 100, .05, .3, 1, 10000)
+    assert row["Method"] == "Serial_vanilla"
+    assert float(row["Result"]) == orc.ref_binom_vanilla_amer(100, 100, .05, .3, 1, 10000, -1.0)
+    row = run("binom_vanilla_eur", "call", 100, 110, .02, .75, 1, 3000)
+    assert float(row["Result"]) == orc.ref_binom_vanilla_eur(100, 110, .02, .75, 1, 3000, 1.0)
