@@ -18,7 +18,7 @@
 //   binom_embar[_omp|_mpi|_hybrid]   payoff S0 E r sigma T N [threads]
 //   binom_vanilla_eur, binom_vanilla_amer   payoff S0 E r sigma T N
 // The threads argument is accepted and reported in the Parallel column, as
-// the reference's OpenMP (threads), MPI (ranks: 1 here) and hybrid
+// the reference's OpenMP (threads), MPI (ranks) and hybrid
 // (ranks*1000 + threads) programs report it.
 //
 // Environment (all optional):
@@ -36,6 +36,8 @@
 //   PCF_METHOD           replaces the Method column (default: the
 //                        reference's label of the variant invoked)
 //   PCF_DEVICE           CUDA device (default 0)
+//   PCF_RANKS            the process count the MPI and hybrid programs report
+//                        (default 1: one process drives the GPU)
 // Errors: the reference throws std::invalid_argument (an unknown payoff, an
 // odd LSM path count, a singular regression) and aborts. Here the message
 // goes to stderr and the exit status is 1.
@@ -192,10 +194,12 @@ int main(int argc, char** argv) {
     next = 9;
   }
   if (var.threads_arg && !arg_i(av, ac, next, &threads)) return fail("invalid numeric argument");
+  const char* rk = getenv("PCF_RANKS");
+  const long long ranks = rk && *rk ? atoll(rk) : 1;
   long long parallel = 0;
   if (strcmp(var.label, "OMP") == 0) parallel = threads;
-  else if (strcmp(var.label, "MPI") == 0) parallel = 1;
-  else if (strcmp(var.label, "Hybrid") == 0) parallel = 1000 + threads;
+  else if (strcmp(var.label, "MPI") == 0) parallel = ranks;
+  else if (strcmp(var.label, "Hybrid") == 0) parallel = ranks * 1000 + threads;
 
   // src/mc_eur.cpp:38-41: call -> 1, put -> -1, anything else is an error.
   int pf;

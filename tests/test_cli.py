@@ -56,3 +56,22 @@ def test_first_argument_selects_the_program(bindir):
         assert len(r.stdout.strip().split(",")) == 16
     else:
         assert r.returncode == 1 and r.stderr.strip()
+
+
+def test_sweep_grids_follow_the_reference_scripts():
+    from parcompfin_gb300 import sweeps
+    # runscript_mc_eur.sh: 18 path counts; serial, 5 thread counts, 5 process
+    # counts, 3 hybrid shapes.
+    runs = sweeps.commands("mc_eur")
+    assert len(runs) == 18 * (1 + 5 + 5 + 3)
+    assert runs[0] == ("mc_eur", ["call", "100", "110", "0.02", "0.75", "1", "10000"], 1)
+    assert runs[18] == ("mc_eur_omp", ["call", "100", "110", "0.02", "0.75", "1", "10000", "1"], 1)
+    assert runs[-1][0] == "mc_eur_hybrid" and runs[-1][2] == 8
+    # runscript_mc_asia.sh has its serial loop commented out.
+    assert all(p != "mc_asia" for p, _, _ in sweeps.commands("mc_asia"))
+    # runscript_binom_embar.sh runs the vanilla lattice beside each serial run.
+    b = sweeps.commands("binom_embar", variants=("serial",))
+    assert [p for p, _, _ in b[:2]] == ["binom_embar", "binom_vanilla_eur"]
+    m = sweeps.commands("mc_eur_multi", max_n=10000, variants=("serial",))
+    assert m == [("mc_eur_multi", ["call", "100", "100", "0.1", "0.2", "1", "10000", "4", "0.5"],
+                  1)]

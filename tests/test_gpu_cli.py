@@ -92,3 +92,18 @@ def test_vanilla_lattice_programs(orc):
     assert float(row["Result"]) == orc.ref_binom_vanilla_amer(100, 100, .05, .3, 1, 10000, -1.0)
     row = run("binom_vanilla_eur", "call", 100, 110, .02, .75, 1, 3000)
     assert float(row["Result"]) == orc.ref_binom_vanilla_eur(100, 110, .02, .75, 1, 3000, 1.0)
+
+
+def test_a_small_sweep_writes_the_reference_csv(tmp_path):
+    from parcompfin_gb300 import sweeps
+    out = tmp_path / "results_mc_amer.csv"
+    n = sweeps.run_sweep("mc_amer", str(out), max_n=80000, variants=("serial", "mpi"), seed=3)
+    lines = out.read_text().strip().split("\n")
+    assert lines[0] == sweeps.HEADER and len(lines) == n + 1 == 1 + 2 + 2 * 5
+    rows = [dict(zip(COLS, ln.split(","))) for ln in lines[1:]]
+    assert rows[0]["Method"] == "Serial" and rows[2]["Method"] == "MPI"
+    assert [r["Parallel"] for r in rows[2:7]] == ["1", "8", "16", "32", "64"]
+    # compared against the GPU lattice American price at N = 10000: with no
+    # dividends the American call is the European call (Black-Scholes 26.6122)
+    lat = float(rows[0]["Result"]) - float(rows[0]["Error"])
+    assert abs(lat - 26.6122) < 0.01
