@@ -59,8 +59,8 @@ namespace pcf {
 
 namespace {
 
-constexpr int kLsmBlock = 512;
-constexpr int kLsmWarps = kLsmBlock / 32;
+constexpr int kLsmBlock = 512;     // cooperative kernel: one block per SM
+constexpr int kLsmCBlock = 512;    // cluster kernel: two CTAs per SM
 constexpr int kRegSums = 8;      // n, x, x^2, x^3, x^4, y, y x, y x^2
 constexpr int kMaxCluster = 16;  // CTAs per contract in a cluster launch
 
@@ -139,9 +139,11 @@ __device__ __forceinline__ LsmSmem<TauT> carve(unsigned char* base, int PB, int 
   return s;
 }
 
-// Static shared memory of one block: the exchange of regression sums.
+// Static shared memory of one block of NW warps: the exchange of regression
+// sums.
+template <int NW>
 struct LsmShared {
-  float wpart[kLsmWarps][kRegSums];              // per-warp FP32 sums
+  float wpart[NW][kRegSums];                     // per-warp FP32 sums
   alignas(16) DF xin[2][kMaxCluster][kRegSums];  // cluster: every CTA's totals, by date parity
   alignas(16) DF ctot[kRegSums];                 // this CTA's totals
   uint64_t xbar[2];                              // cluster: bytes of the CTAs' totals
@@ -150,7 +152,7 @@ struct LsmShared {
   float coef[3];
   int mode;  // 0 skip the date, 1 few in-the-money paths, 2 regression
   int fail;  // a wait gave up
-  DF sh[kLsmWarps * kMoments];
+  DF sh[NW * kMoments];
   DF fin[kMoments];
 };
 
@@ -236,8 +238,8 @@ __device__ __forceinline__ bool group_arrive_wait(unsigned* counter, unsigned G,
 // Date d's regression, run by warp 0 between the two block barriers: the
 // block's total of each sum, the exchange of block totals, the contract's
 // sums in FP64 and the solve. Leaves the mode and coefficients in X.
-template <bool CLUSTER>
-__device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared& X, int d, int b,
+template <bool CLUSTER, int NW>
+__device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& X, int d, int b,
                                              uint32_t& xph) {
   const int lane = threadIdx.x & 31;
   const int q = lane & 7;
@@ -245,7 +247,7 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared& X, i
   // then two shuffle steps combine the groups. Lanes 0..7 hold the totals.
   DF v = DF{X.wpart[lane >> 3][q], 0.f};
 #pragma unroll
-  for (int w = (lane >> 3) + 4; w < kLsmWarps; w += 4) v = df_add_f(v, X.wpart[w][q]);
+  for (int w = (lane >> 3) + 4; w < NW; w += 4) v = df_add_f(v, X.wpart[w][q]);
   v = df_add(v, shfl_xor_df(v, 8));
   v = df_add(v, shfl_xor_df(v, 16));
   const int slot = d & 1;
@@ -362,19 +364,19 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared& X, i
 // cooperative block that gave up leaves after its in-flight copies landed; a
 // cluster CTA records the failure and keeps taking part in every exchange and
 // cluster barrier (a hardware barrier has no timeout), so no CTA leaves early.
-template <bool CLUSTER, typename TauT>
+template <bool CLUSTER, typename TauT, int BS>
 __device__ void lsm_body(const LsmParams& P, int b) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int PB = P.pairs_per_block;
   const int M = P.M;
   const LsmSmem<TauT> S = carve<TauT>(smem_raw, PB, M);
-  __shared__ LsmShared X;
+  __shared__ LsmShared<BS / 32> X;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 
   const long long p0 = (long long)b * PB;
   const int nb = (int)max(0LL, min((long long)PB, P.H - p0));  // pairs in this block
   const int nbr = (nb + 3) & ~3;                                // bulk-copy width
-  for (int k = threadIdx.x; k <= M; k += kLsmBlock) {
+  for (int k = threadIdx.x; k <= M; k += BS) {
     S.dt[k] = P.dtab[k];
     S.edt[k] = P.dtab[M + 1 + k];
   }
@@ -395,7 +397,7 @@ __device__ void lsm_body(const LsmParams& P, int b) {
   const size_t stride = (size_t)2 * P.Hp;  // floats per row
   const float nb2 = -P.b2;
 #pragma unroll 2
-  for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+  for (int i = threadIdx.x; i < nb; i += BS) {
     const long long p = p0 + i;
     float Lp = 0.f, Lm = 0.f, Sp = 0.f, Sm = 0.f;
     float* row = P.paths + p;
@@ -458,7 +460,7 @@ __device__ void lsm_body(const LsmParams& P, int b) {
       if (threadIdx.x == 32) issue_row(P, next_row, p0, nbr, PB, S.slice(next_k), &S.bar[next_k]);
       pend |= 1u << next_k;
     }
-    if (wid == 0) regress_date<CLUSTER>(P, X, d, b, xph);
+    if (wid == 0) regress_date<CLUSTER, BS / 32>(P, X, d, b, xph);
     __syncthreads();
   };
 
@@ -470,7 +472,7 @@ __device__ void lsm_body(const LsmParams& P, int b) {
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
     const float* sl = S.slice(0);
     const float e1 = S.edt[M - 1];
-    for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+    for (int i = threadIdx.x; i < nb; i += BS) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + i;
@@ -495,7 +497,7 @@ __device__ void lsm_body(const LsmParams& P, int b) {
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
 #pragma unroll 2
-    for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+    for (int i = threadIdx.x; i < nb; i += BS) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + i;
@@ -545,7 +547,7 @@ __device__ void lsm_body(const LsmParams& P, int b) {
   // money) and S_M from the last row otherwise.
   const float* last = P.paths + (size_t)(M - 1) * 2 * P.Hp;
   KSum sy, syy, sg, sgg, syg;
-  for (int i = threadIdx.x; i < nb; i += kLsmBlock) {
+  for (int i = threadIdx.x; i < nb; i += BS) {
     float y2 = 0.f, g2 = 0.f;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -596,19 +598,21 @@ __device__ void lsm_body(const LsmParams& P, int b) {
 }
 
 __global__ void __launch_bounds__(kLsmBlock, 1) lsm_kernel(LsmParams P) {
-  lsm_body<false, unsigned short>(P, blockIdx.x);
+  lsm_body<false, unsigned short, kLsmBlock>(P, blockIdx.x);
 }
 
 // Many contracts in one launch, one thread-block cluster per contract
-// (cluster size = the contracts' common CTA count). Two CTAs per SM.
+// (cluster size = the contracts' common CTA count). Two CTAs per SM: while
+// one runs its per-date exchange and solve, the other's paths keep the SM
+// busy.
 template <typename TauT>
-__global__ void __launch_bounds__(kLsmBlock, 2) lsm_cluster_kernel(const LsmParams* __restrict__ cs) {
+__global__ void __launch_bounds__(kLsmCBlock, 2) lsm_cluster_kernel(const LsmParams* __restrict__ cs) {
   __shared__ LsmParams sP;  // the contract's parameters, read from shared memory
   const unsigned rank = cg::this_cluster().block_rank();
   const int c = (int)(blockIdx.x / cg::this_cluster().num_blocks());
   if (threadIdx.x == 0) sP = cs[c];
   __syncthreads();
-  lsm_body<true, TauT>(sP, (int)rank);
+  lsm_body<true, TauT, kLsmCBlock>(sP, (int)rank);
 }
 
 // Dynamic shared memory of one block (the carve above).
@@ -724,7 +728,7 @@ const LsmLimits& lsm_limits(const pcf_ctx* c) {
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(16);
-    cfg.blockDim = dim3(kLsmBlock);
+    cfg.blockDim = dim3(kLsmCBlock);
     cfg.dynamicSmemBytes = lsm_smem(4096, 64, 1);
     cfg.attrs = at;
     cfg.numAttrs = 1;
@@ -765,6 +769,8 @@ constexpr int kNumPB = 5;
 // smallest such slice at that cluster size); beyond that, the largest cluster
 // with one CTA per SM. Few CTAs per contract leave room for more contracts in
 // flight, and each CTA pays the per-date exchange once for more paths.
+// (Measured: one 1024-thread CTA per SM holding the same 8192 pairs ran the
+// 64-put batch no faster and the mixed stream 4 % slower.)
 bool cluster_shape(const LsmLimits& Lm, long long H, int M, int& cl, int& k, bool& t8) {
   t8 = M <= 255;
   const size_t tb = t8 ? 1 : 2, stat = t8 ? Lm.stat8 : Lm.stat16;
@@ -998,7 +1004,7 @@ int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(L.C * L.CL);
-    cfg.blockDim = dim3(kLsmBlock);
+    cfg.blockDim = dim3(kLsmCBlock);
     cfg.dynamicSmemBytes = L.smem;
     cfg.stream = s;
     cfg.attrs = at;
