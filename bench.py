@@ -63,6 +63,15 @@ def _sfu_roofline(sfu_per_unit, units, ms, sms, sm_mhz):
                            "under load); compute-bound kernel, no HBM traffic to speak of"}
 
 
+def _fp32_roofline(flop_per_unit, units, ms, sms, sm_mhz):
+    peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s: 128 FP32 FMA lanes per SM
+    ach = flop_per_unit * units / (ms * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": ach / peak, "traffic": None,
+            "peak_source": f"{sms} SMs x 128 FMA lanes x 2 flop x {sm_mhz:.0f} MHz (median SM "
+                           "clock under load)"}
+
+
 # --------------------------------------------------------------------------
 # workloads
 # --------------------------------------------------------------------------
@@ -202,7 +211,7 @@ class BasketWorkload:
     name = "basket"
     metric = "MC paths/sec (basket, d in {4, 16, 64})"
     unit = "paths/s"
-    dominant = "mc_kernel<2,64,...> (basket)"
+    dominant = "mc_basket_tc_kernel<64,...> (basket, L z on the tensor cores)"
 
     def __init__(self, rank):
         import parcompfin_gb300 as pcf
@@ -233,8 +242,18 @@ class BasketWorkload:
                 "paths_per_step": self.units(), "contracts_per_step": len(self.cs)}
 
     def roofline(self, ms, sms, mhz):
+        # Per path: 3 SFU ops per asset (normals, exp) on the CUDA cores. The
+        # L z product (d(d+1) flops) runs on the tensor cores for d > 16
+        # (3xTF32 tcgen05.mma), so the CUDA-core bound is the random stream:
+        # SFU ops and issue. "fp32_equivalent" counts the whole product as if
+        # it ran on the FP32 pipe: d(d+1) + 7.5 d + 11 flops per path.
         sfu = sum(c["N"] * 3.0 * c["assets"] for c in self.cs) / self.units()
-        return _sfu_roofline(sfu, self.units(), ms, sms, mhz)
+        d_flop = lambda d: d * (d + 1) + 7.5 * d + 11
+        flop = sum(c["N"] * d_flop(c["assets"]) for c in self.cs) / self.units()
+        a = _sfu_roofline(sfu, self.units(), ms, sms, mhz)
+        b = _fp32_roofline(flop, self.units(), ms, sms, mhz)
+        a["fp32_equivalent"] = {k: b[k] for k in ("achieved", "peak", "unit", "frac")}
+        return a
 
     def cpu_reference(self, threads, budget_s):
         # The reference's basket needs Eigen and Boost (include/mvn.h), absent

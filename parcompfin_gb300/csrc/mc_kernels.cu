@@ -20,6 +20,8 @@
 //   European  src/mc_eur.cpp:22-26,  src/mc_eur_omp.cpp:24-27
 //   Asian     src/mc_asia.cpp:26-39, src/mc_asia_omp.cpp:33-44
 //   basket    src/mc_eur_multi.cpp:19-34 with include/mvn.h:42-82
+#include <algorithm>
+
 #include "pcf_device.cuh"
 #include "pcf_internal.h"
 
@@ -144,49 +146,52 @@ __device__ __forceinline__ void asia_item(const McContract& C, int j, Moments<CV
 // shared memory; log2 S_a = l0_a + v_a x_a; y = payoff(mean_a S_a),
 // g = payoff(2^(mean_a log2 S_a)). mode 0: the factor is lower triangular
 // (Cholesky); mode 1: a full factor (eigen-decomposition fallback).
+// The staged block is fb = [l0 | v | L], each row of L padded to DMAX floats
+// with zeros beyond the factor, 16-byte aligned. The product runs column
+// group by column group: the four normals of group b are drawn and folded
+// into every row accumulator x_a that group touches (a >= 4b for the
+// triangular factor), one 16-byte load of L per row and group. So the normals
+// are never held as an array, the row accumulators are independent FMA
+// chains, and the triangle costs exactly its FMAs (groups beyond d are
+// skipped by uniform branches). Each x_a is the sum over b = 0, 1, ... in
+// order, and the padding adds exact zeros.
 template <int DMAX, bool CV>
 __device__ __forceinline__ void basket_path(const McContract& C, const float* fb, long long n,
                                             Moments<CV>& mo) {
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_BASKET};
   const int d = C.M;
   const float* l0 = fb;
-  const float* vol = fb + d;
-  const float* Lf = fb + 2 * d;
-  float z[DMAX];
+  const float* vol = fb + DMAX;
+  const float* Lf = fb + 2 * DMAX;
+  const bool tri = C.mode == 0;
+  float x[DMAX];
 #pragma unroll
-  for (int a0 = 0; a0 < DMAX; a0 += 4) {
-    if (a0 < d) {
-      const float4 zz = normals4(draw_words(key, (uint64_t)n, (uint32_t)(a0 >> 2)));
-      z[a0] = zz.x;
-      z[a0 + 1] = zz.y;
-      z[a0 + 2] = zz.z;
-      z[a0 + 3] = zz.w;
-    } else {
-      z[a0] = z[a0 + 1] = z[a0 + 2] = z[a0 + 3] = 0.f;
+  for (int a = 0; a < DMAX; ++a) x[a] = 0.f;
+#pragma unroll
+  for (int b4 = 0; b4 < DMAX / 4; ++b4) {
+    if (4 * b4 < d) {
+      const float4 z = normals4(draw_words(key, (uint64_t)n, (uint32_t)b4));
+#pragma unroll
+      for (int a4 = 0; a4 < DMAX / 4; ++a4) {
+        if (4 * a4 < d && (a4 >= b4 || !tri)) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int a = 4 * a4 + j;
+            const float4 l = *reinterpret_cast<const float4*>(Lf + a * DMAX + 4 * b4);
+            x[a] = fmaf(l.x, z.x, x[a]);
+            x[a] = fmaf(l.y, z.y, x[a]);
+            x[a] = fmaf(l.z, z.z, x[a]);
+            x[a] = fmaf(l.w, z.w, x[a]);
+          }
+        }
+      }
     }
   }
   float bsk = 0.f, geo = 0.f;
-  if (C.mode == 0) {  // lower-triangular Cholesky factor
 #pragma unroll
-    for (int a = 0; a < DMAX; ++a) {
-      if (a < d) {
-        const float* row = Lf + a * d;
-        float x = 0.f;
-#pragma unroll
-        for (int b = 0; b <= a; ++b) x = fmaf(row[b], z[b], x);
-        const float l2 = fmaf(vol[a], x, l0[a]);
-        bsk += ex2_approx(l2);
-        geo += l2;
-      }
-    }
-  } else {  // full factor from the eigen-decomposition fallback
-    for (int a = 0; a < d; ++a) {
-      const float* row = Lf + a * d;
-      float x = 0.f;
-#pragma unroll
-      for (int b = 0; b < DMAX; ++b)
-        if (b < d) x = fmaf(row[b], z[b], x);
-      const float l2 = fmaf(vol[a], x, l0[a]);
+  for (int a = 0; a < DMAX; ++a) {
+    if (a < d) {
+      const float l2 = fmaf(vol[a], x[a], l0[a]);
       bsk += ex2_approx(l2);
       geo += l2;
     }
@@ -233,11 +238,12 @@ __device__ __forceinline__ int find_contract(const int* start, int n, int item) 
 // one of the next 255, so each thread tests one candidate (a binary search
 // covers longer jumps).
 template <int METHOD, int DMAX, bool CV>
-__global__ void __launch_bounds__(kBlock) mc_kernel(McLaunch L) {
+__global__ void __launch_bounds__(kBlock, DMAX >= 64 ? 2 : (METHOD == MC_EUR ? 5 : 4))
+mc_kernel(McLaunch L) {
   __shared__ DF sh[32 * kMoments];
   __shared__ int s_item[2];
   __shared__ int s_c;
-  extern __shared__ float s_fb[];
+  extern __shared__ __align__(16) float s_fb[];
   if (threadIdx.x == 0) {
     s_c = -1;
     if (L.persistent) s_item[0] = (int)atomicAdd(L.queue, 1u);
@@ -277,9 +283,19 @@ __global__ void __launch_bounds__(kBlock) mc_kernel(McLaunch L) {
       asia_item<CV>(C, j, mo);
     } else {
       if (loaded != c) {  // the previous item's readers are past the final barrier
+        // Host layout [l0 (d) | v (d) | L (d x d)] -> padded [l0 | v | L rows of DMAX].
         const int d = C.M;
         const float* src = L.basket_data + C.basket_off;
-        for (int i = threadIdx.x; i < 2 * d + d * d; i += kBlock) s_fb[i] = src[i];
+        for (int i = threadIdx.x; i < (2 + DMAX) * DMAX; i += kBlock) {
+          const int row = i / DMAX, col = i % DMAX;
+          float v = 0.f;
+          if (row < 2) {
+            if (col < d) v = src[row * d + col];
+          } else if (row - 2 < d && col < d) {
+            v = src[2 * d + (row - 2) * d + col];
+          }
+          s_fb[i] = v;
+        }
         __syncthreads();
         loaded = c;
       }
@@ -295,7 +311,301 @@ __global__ void __launch_bounds__(kBlock) mc_kernel(McLaunch L) {
   }
 }
 
-constexpr size_t basket_smem(int dmax) { return (size_t)(2 * dmax + dmax * dmax) * sizeof(float); }
+// ---- baskets of more than 16 assets: the L z product on the tensor cores ----
+//
+// A tile is 128 paths (one per thread); the product X = Z L^T of a tile runs
+// on the tensor cores, K (the assets) in chunks of 8. For each chunk every
+// thread draws its path's next 8 normals and stores them, split into two
+// TF32 parts z = z_hi + z_lo, as row `tid` of a 128 x 8 K-major chunk in
+// shared memory (double-buffered); one thread then issues three
+// tcgen05.mma kind::tf32 (M = 128, N = d rounded up to 16, K = 8)
+// accumulating X += Z_hi L_hi^T + Z_lo L_hi^T + Z_hi L_lo^T in tensor memory
+// and commits them to the chunk buffer's mbarrier, so drawing chunk c + 1
+// overlaps the MMAs of chunk c. The dropped Z_lo L_lo^T term is below 2^-22
+// of the product: X carries FP32-level accuracy. The factor is staged once
+// per contract, split the same way. After the last chunk each warp reads its
+// 32 rows of X (tcgen05.ld 32x32b) and finishes its paths on the CUDA cores.
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8-row x 16-byte core matrices, adjacent along K 128 bytes apart (leading
+// offset) and along M/N (K/4) x 128 bytes apart (stride offset). A chunk
+// buffer is 16 KB, so four CTAs share an SM.
+constexpr int kTcBlock = 128;
+
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int ktot) {
+  return (uint32_t)((row >> 3) * (ktot >> 2) * 128 + (k >> 2) * 128 + (row & 7) * 16 +
+                    (k & 3) * 4);
+}
+
+// Shared-memory matrix descriptor (no swizzle, descriptor version 1).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar)));
+}
+
+// 32 consecutive accumulator columns of this thread's row (its warp's lanes).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+constexpr int kTcChunk = kTcBlock * 8;  // floats in one 128 x 8 chunk
+
+template <int DMAX>
+constexpr size_t tc_basket_smem() {  // l0, v | L_hi, L_lo | 2 x (Z_hi, Z_lo) chunks (floats)
+  return (size_t)(2 * DMAX + 2 * DMAX * DMAX + 4 * kTcChunk) * sizeof(float);
+}
+
+template <int DMAX, bool CV>
+__global__ void __launch_bounds__(kTcBlock, 4) mc_basket_tc_kernel(McLaunch L) {
+  static_assert(DMAX == 32 || DMAX == 64, "tensor-core baskets: 17..64 assets");
+  extern __shared__ __align__(128) float s_tc[];
+  __shared__ DF sh[32 * kMoments];
+  __shared__ int s_item[2];
+  __shared__ int s_c;
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t s_tmem;
+  float* l0 = s_tc;
+  float* vol = s_tc + DMAX;
+  float* Lhi = s_tc + 2 * DMAX;
+  float* Llo = Lhi + DMAX * DMAX;
+  float* Zc = Llo + DMAX * DMAX;  // buffer b: Z_hi at Zc + 2 b chunk, Z_lo next to it
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&s_tmem)),
+                 "r"(DMAX));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    s_c = -1;
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+    if (L.persistent) s_item[0] = (int)atomicAdd(L.queue, 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = s_tmem;
+  const uint32_t row_tmem = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t sbo_l = (DMAX / 4) * 128;
+  const uint32_t z_off = kmajor_off(tid, 0, 8) >> 2;  // this thread's row in a chunk
+  uint32_t phase = 0;   // bit b: parity of the next wait on mbar[b]
+  uint32_t pending = 0; // bit b: a commit on mbar[b] not yet waited
+  bool failed = false;
+  auto wait_buf = [&](int b) {
+    if (!((pending >> b) & 1u)) return;
+    if (!mbar_poll(&mbar[b], (phase >> b) & 1u, 1u << 24)) failed = true;
+    phase ^= 1u << b;
+    pending &= ~(1u << b);
+  };
+  int c = 0, loaded = -1;
+  for (int iter = 0;; ++iter) {
+    int item;
+    if (L.persistent) {
+      item = s_item[iter & 1];
+      if (tid == 0 && item < L.total_items) s_item[(iter + 1) & 1] = (int)atomicAdd(L.queue, 1u);
+    } else {
+      if (iter > 0) break;
+      item = blockIdx.x;
+    }
+    if (item >= L.total_items) break;
+    {
+      const int t = c + tid;
+      if (t < L.ncontracts && __ldg(L.item_start + t) <= item &&
+          (t + 1 == L.ncontracts || item < __ldg(L.item_start + t + 1)))
+        s_c = t;
+      __syncthreads();
+      const int found = s_c;
+      c = found >= 0 ? found : find_contract(L.item_start, L.ncontracts, item);
+    }
+    const McContract C = L.contracts[c];
+    const int base = __ldg(L.item_start + c);
+    const int j = item - base;
+    const int d = C.M;
+    if (loaded != c) {
+      // Every MMA has completed (the last tile waited for all of them).
+      // Host layout [l0 (d) | v (d) | L (d x d)]; L rows are the MMA's N rows.
+      const float* src = L.basket_data + C.basket_off;
+      for (int i = tid; i < DMAX; i += kTcBlock) {
+        l0[i] = i < d ? src[i] : 0.f;
+        vol[i] = i < d ? src[d + i] : 0.f;
+      }
+      for (int i = tid; i < DMAX * DMAX; i += kTcBlock) {
+        const int n = i / DMAX, k = i % DMAX;
+        const float v = (n < d && k < d) ? src[2 * d + n * d + k] : 0.f;
+        const float hi = tf32_round(v);
+        const uint32_t o = kmajor_off(n, k, DMAX) >> 2;
+        Lhi[o] = hi;
+        Llo[o] = tf32_round(v - hi);
+      }
+      loaded = c;
+    }
+    const int nchunks = (d + 7) >> 3, np = (d + 15) & ~15;
+    // D f32, A and B tf32, both K-major; N >> 3 at bit 17, M >> 4 at bit 24.
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(np >> 3) << 17) |
+                           ((uint32_t)(kTcBlock >> 4) << 24);
+    const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_BASKET};
+    Moments<CV> mo;
+    for (int tile = 0; tile < C.units_per_item / kTcBlock; ++tile) {
+      const long long n = (long long)j * C.units_per_item + (long long)tile * kTcBlock + tid;
+      for (int ch = 0; ch < nchunks; ++ch) {
+        const int b = ch & 1;
+        wait_buf(b);  // the MMAs that read buffer b two chunks ago are done
+        float* zh = Zc + 2 * b * kTcChunk;
+        float* zl = zh + kTcChunk;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int k4 = 2 * ch + h;
+          float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (4 * k4 < d) z = normals4(draw_words(key, (uint64_t)n, (uint32_t)k4));
+          const float4 hi = make_float4(tf32_round(z.x), tf32_round(z.y), tf32_round(z.z),
+                                        tf32_round(z.w));
+          const float4 lo = make_float4(tf32_round(z.x - hi.x), tf32_round(z.y - hi.y),
+                                        tf32_round(z.z - hi.z), tf32_round(z.w - hi.w));
+          *reinterpret_cast<float4*>(zh + z_off + 32 * h) = hi;  // +128 bytes: next core matrix
+          *reinterpret_cast<float4*>(zl + z_off + 32 * h) = lo;
+        }
+        // The chunk (and a newly staged factor) is visible to the tensor core;
+        // at ch = 0 every thread has also read the previous tile's X.
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) {
+          const uint32_t ah = smem_u32(zh), al = smem_u32(zl);
+          const uint32_t bo = (uint32_t)ch * 256;  // chunk ch: two core matrices along K
+          const uint32_t bh = smem_u32(Lhi) + bo, bl = smem_u32(Llo) + bo;
+          umma_tf32(tmem, umma_desc(ah, 128, 256), umma_desc(bh, 128, sbo_l), idesc, ch > 0);
+          umma_tf32(tmem, umma_desc(al, 128, 256), umma_desc(bh, 128, sbo_l), idesc, 1);
+          umma_tf32(tmem, umma_desc(ah, 128, 256), umma_desc(bl, 128, sbo_l), idesc, 1);
+          umma_commit(&mbar[b]);
+        }
+        pending |= 1u << b;
+      }
+      wait_buf(0);
+      wait_buf(1);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      float bsk = 0.f, geo = 0.f;
+#pragma unroll
+      for (int half = 0; half < DMAX / 32; ++half) {
+        if (32 * half < np) {
+          float x[32];
+          tmem_ld32(row_tmem + 32 * half, x);
+#pragma unroll
+          for (int a = 0; a < 32; ++a) {
+            if (32 * half + a < d) {
+              const float l2 = fmaf(vol[32 * half + a], x[a], l0[32 * half + a]);
+              bsk += ex2_approx(l2);
+              geo += l2;
+            }
+          }
+        }
+      }
+      if (n < C.N) {
+        const float inv_d = 1.f / (float)d;
+        float Y = payoff(C, bsk * inv_d);
+        float G = CV ? payoff(C, ex2_approx(geo * inv_d)) : 0.f;
+        if (failed) Y = G = __int_as_float(0x7fc00000);  // a wait gave up: the result is NaN
+        mo.add(Y, G);
+      }
+    }
+    DF v[kMoments] = {df_of(mo.y), df_of(mo.yy), df_of(mo.g), df_of(mo.gg), df_of(mo.yg)};
+    DF tot[kMoments];
+    block_sum_df<kMoments>(v, sh, tot);
+    grid_finalize_df<kMoments>(tot, (float2*)L.partial + (size_t)base * kMoments, L.tickets + c,
+                               L.out + (size_t)c * kMoments, C.items, j);
+    if (tid == 0) s_c = -1;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DMAX));
+  }
+}
+
+// Dynamic shared memory above 48 KB and the largest shared-memory carveout,
+// so that four CTAs share an SM.
+template <int DMAX, bool CV>
+void tc_setup() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(mc_basket_tc_kernel<DMAX, CV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tc_basket_smem<DMAX>());
+  cudaFuncSetAttribute(mc_basket_tc_kernel<DMAX, CV>,
+                       cudaFuncAttributePreferredSharedMemoryCarveout,
+                       (int)cudaSharedmemCarveoutMaxShared);
+  done = true;
+}
+
+template <int DMAX, bool CV>
+cudaError_t launch_tc(const McLaunch& L, int grid, cudaStream_t s) {
+  tc_setup<DMAX, CV>();
+  mc_basket_tc_kernel<DMAX, CV><<<grid, kTcBlock, tc_basket_smem<DMAX>(), s>>>(L);
+  return cudaGetLastError();
+}
+
+// CTAs per SM: the launch bound (4) caps the registers; shared memory
+// decides the rest. (The occupancy query reports one CTA per SM for this
+// kernel, which leaves three quarters of each SM idle; a persistent launch
+// of more CTAs than fit would only queue them.)
+template <int DMAX>
+int tc_max_active(void) {
+  tc_setup<DMAX, true>();
+  tc_setup<DMAX, false>();
+  int dev = 0, smem_sm = 0, reserved = 0;
+  cudaFuncAttributes fa;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
+          cudaSuccess ||
+      cudaFuncGetAttributes(&fa, mc_basket_tc_kernel<DMAX, true>) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  const size_t per = tc_basket_smem<DMAX>() + fa.sharedSizeBytes + (size_t)reserved;
+  return std::max(1, std::min(4, (int)((size_t)smem_sm / per)));
+}
+
+constexpr size_t basket_smem(int dmax) { return (size_t)(2 + dmax) * dmax * sizeof(float); }
 
 template <int METHOD, int DMAX, bool CV>
 cudaError_t launch_one(const McLaunch& L, int grid, cudaStream_t s) {
@@ -331,8 +641,8 @@ cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, cudaSt
       if (max_d <= 4) return launch_cv<MC_BASKET, 4>(L, grid, s);
       if (max_d <= 8) return launch_cv<MC_BASKET, 8>(L, grid, s);
       if (max_d <= 16) return launch_cv<MC_BASKET, 16>(L, grid, s);
-      if (max_d <= 32) return launch_cv<MC_BASKET, 32>(L, grid, s);
-      if (max_d <= 64) return launch_cv<MC_BASKET, 64>(L, grid, s);
+      if (max_d <= 32) return L.cv ? launch_tc<32, true>(L, grid, s) : launch_tc<32, false>(L, grid, s);
+      if (max_d <= 64) return L.cv ? launch_tc<64, true>(L, grid, s) : launch_tc<64, false>(L, grid, s);
       return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;
@@ -346,8 +656,8 @@ int mc_max_active_blocks(McMethod m, int max_d) {
       if (max_d <= 4) return max_active<MC_BASKET, 4>();
       if (max_d <= 8) return max_active<MC_BASKET, 8>();
       if (max_d <= 16) return max_active<MC_BASKET, 16>();
-      if (max_d <= 32) return max_active<MC_BASKET, 32>();
-      return max_active<MC_BASKET, 64>();
+      if (max_d <= 32) return tc_max_active<32>();
+      return tc_max_active<64>();
   }
   return 1;
 }

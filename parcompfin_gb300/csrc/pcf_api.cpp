@@ -204,8 +204,9 @@ int eur_quads_per_thread(long long N) {
 int asia_paths_per_thread(int M) { return std::max(1, std::min(16, (256 + M - 1) / M)); }
 
 // Basket: a few paths per thread for baskets of up to 8 assets (the kernels
-// for wider baskets take one path per thread).
-int basket_paths_per_thread(int d) { return d <= 4 ? 8 : d <= 8 ? 4 : 1; }
+// for 9..16 assets take one path per thread); wider baskets run the
+// tensor-core kernel, whose items are 8 tiles of 128 paths.
+int basket_paths_per_thread(int d) { return d <= 4 ? 8 : d <= 8 ? 4 : d <= 16 ? 1 : 4; }
 
 McContract make_eur(double S0, double E, double r, double sigma, double T, long long N, int pf,
                     unsigned long long seed, uint32_t stream) {

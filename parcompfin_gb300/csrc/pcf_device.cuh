@@ -344,6 +344,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// mbar_wait without the hardware suspend of try_wait: polls test_wait, for
+// waits that usually end within a few hundred cycles. Bounded.
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
 // ---- exchanges between the CTAs of a thread-block cluster ----
 // Address of the same shared-memory object in CTA `rank` of the cluster.
 __device__ __forceinline__ uint32_t cluster_map(const void* p, uint32_t rank) {

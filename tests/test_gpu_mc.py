@@ -158,7 +158,9 @@ def _chol(corr, d):
     return L
 
 
-@pytest.mark.parametrize("d", [1, 4, 7, 16, 33, 64])
+# d > 16 runs the tensor-core kernel (3xTF32 products): 17, 24 and 48 leave
+# padded K and N, 32 and 64 fill them exactly.
+@pytest.mark.parametrize("d", [1, 4, 7, 16, 17, 24, 32, 33, 48, 64])
 def test_basket_matches_fp64_twin(orc, ctx, d):
     from parcompfin_gb300 import mc_basket_result
     import random
@@ -186,6 +188,41 @@ def test_basket_reference_article_values(ctx):
     ref_se = res.std_error_plain * math.sqrt((1 << 24) / 1e8)
     se = math.hypot(res.std_error_cv, ref_se)
     assert abs(res.price_cv - 11.9205) < 3 * se + 5e-5, (res.price_cv, se)
+
+
+def test_wide_baskets_share_one_launch(orc, ctx):
+    """Baskets of 20, 40 and 64 assets in one batch: the tensor-core kernel
+    stages each contract's factor in turn; every contract matches its twin."""
+    import parcompfin_gb300 as pcf
+    import random
+    reqs, args = [], []
+    for i, d in enumerate((20, 40, 64)):
+        rng = random.Random(100 + d)
+        S0 = [100.0 + rng.uniform(-5, 5) for _ in range(d)]
+        sig = [rng.uniform(.15, .35) for _ in range(d)]
+        corr = [1.0 if a == b else .25 for a in range(d) for b in range(d)]
+        reqs.append(pcf.request("basket", 100, 100, .03, .25, 1.0, 30000, "call", assets=d,
+                                basket_S0=S0, basket_sigma=sig, corr=corr, use_cv=True,
+                                scale_by_sqrt_T=True, seed=21, stream=i))
+        args.append((d, S0, sig, corr))
+    out = pcf.price_batch(reqs, ctx=ctx)
+    for (d, S0, sig, corr), r, i in zip(args, out, range(3)):
+        s = (C.c_double * 5)()
+        A = C.c_double * d
+        orc.twin_mc_basket(d, A(*S0), A(*sig), (C.c_double * (d * d))(*_chol(corr, d)), .03, 1.0,
+                           1.0, 100.0, 30000, 1, 21, i, s)
+        for k in range(5):
+            assert rel(r.sums[k], s[k]) < DET_REL, (d, k, r.sums[k], s[k])
+
+
+def test_wide_basket_eigen_fallback(ctx):
+    """A rank-one correlation of 24 assets takes the full (eigen) factor on
+    the tensor-core path; identical assets with rho = 1 are one asset."""
+    from parcompfin_gb300 import mc_basket_result
+    d = 24
+    res = mc_basket_result([100.0] * d, [.2] * d, [1.0] * (d * d), .05, 1.0, 100.0, 1 << 20, 1,
+                           seed=9, use_cv=True, ctx=ctx)
+    assert abs(res.price_cv - 10.450583572185565) < 4 * res.std_error_cv + 1e-4
 
 
 def test_basket_eigen_fallback(ctx):
