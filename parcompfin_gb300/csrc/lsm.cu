@@ -995,6 +995,11 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
 }
 
 int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
+  const int st = lsm_batch_launch_clusters(c, B, s);
+  return st ? st : lsm_batch_launch_coop(c, B, s);
+}
+
+int lsm_batch_launch_clusters(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
   int st;
   for (const LsmCluster& L : B->clusters) {
     cudaLaunchConfig_t cfg = {};
@@ -1016,6 +1021,11 @@ int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
     if (st) return st;
     c->launches += 1;
   }
+  return PCF_OK;
+}
+
+int lsm_batch_launch_coop(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
+  int st;
   for (size_t i = 0; i < B->coop.size(); ++i) {
     LsmParams& P = B->coop[i];
     st = cuda_status(cudaMemsetAsync(P.barrier, 0, 2 * sizeof(unsigned), s), "memset LSM counters");
@@ -1031,6 +1041,7 @@ int lsm_batch_launch(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
 }
 
 int lsm_batch_kernels(const LsmBatch* B) { return (int)(B->clusters.size() + B->coop.size()); }
+int lsm_batch_cluster_kernels(const LsmBatch* B) { return (int)B->clusters.size(); }
 
 void lsm_batch_destroy(LsmBatch* B) {
   if (!B) return;

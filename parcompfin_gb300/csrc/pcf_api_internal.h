@@ -99,7 +99,12 @@ int lsm_batch_bytes(pcf_ctx* c, const std::vector<LsmRequest>& reqs, size_t* dev
 int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream_t s,
                      ExtMem* mem, LsmBatch** out);
 int lsm_batch_launch(pcf_ctx* c, LsmBatch* b, cudaStream_t s);
+// The two parts of lsm_batch_launch: the cluster launches, then the
+// cooperative ones (which need every block resident, so they run alone).
+int lsm_batch_launch_clusters(pcf_ctx* c, LsmBatch* b, cudaStream_t s);
+int lsm_batch_launch_coop(pcf_ctx* c, LsmBatch* b, cudaStream_t s);
 int lsm_batch_kernels(const LsmBatch* b);
+int lsm_batch_cluster_kernels(const LsmBatch* b);
 void lsm_batch_destroy(LsmBatch* b);
 
 }  // namespace pcf

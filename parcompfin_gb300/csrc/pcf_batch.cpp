@@ -280,6 +280,19 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
       return st;
     }
   }
+  if (p->lsm && !p->groups.empty()) {
+    // A failure here only leaves the plan without the fork (sequential launches).
+    if (cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      if (p->side) cudaStreamDestroy(p->side);
+      if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+      if (p->ev_join) cudaEventDestroy(p->ev_join);
+      p->side = nullptr;
+      p->ev_fork = p->ev_join = nullptr;
+    }
+  }
   *out = p;
   return PCF_OK;
 }
@@ -293,11 +306,24 @@ int plan_enqueue(pcf_plan* p) {
                          "memset tickets");
     if (st) return st;
   }
+  const bool fork = p->side && p->lsm && lsm_batch_cluster_kernels(p->lsm) > 0 &&
+                    !p->groups.empty();
+  if (fork) {
+    int st = cuda_status(cudaEventRecord(p->ev_fork, p->stream), "plan fork");
+    if (!st) st = cuda_status(cudaStreamWaitEvent(p->side, p->ev_fork, 0), "plan fork");
+    if (!st) st = lsm_batch_launch_clusters(c, p->lsm, p->side);
+    if (!st) st = cuda_status(cudaEventRecord(p->ev_join, p->side), "plan join");
+    if (st) return st;
+  }
   for (Group& gr : p->groups) {
     int st = cuda_status(launch_mc(gr.method, gr.L, gr.grid, gr.max_d, p->stream),
                          "batch kernel launch");
     if (st) return st;
     c->launches += 1;
+  }
+  if (fork) {
+    const int st = cuda_status(cudaStreamWaitEvent(p->stream, p->ev_join, 0), "plan join");
+    return st ? st : lsm_batch_launch_coop(c, p->lsm, p->stream);
   }
   if (p->lsm) return lsm_batch_launch(c, p->lsm, p->stream);
   return PCF_OK;
@@ -429,6 +455,12 @@ int pcf_plan_destroy(pcf_plan* p) {
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->stream);
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  if (p->side) {
+    cudaStreamSynchronize(p->side);
+    cudaStreamDestroy(p->side);
+  }
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
   lsm_batch_destroy(p->lsm);
   if (p->d_mem) cudaFree(p->d_mem);
   if (p->h_own) cudaFreeHost(p->h_own);

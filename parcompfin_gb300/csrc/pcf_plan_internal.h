@@ -44,6 +44,10 @@ struct pcf_plan {
   int* h_amer_flags = nullptr;
   // CUDA graph replay: the second launch captures the launch sequence, later
   // launches replay it. graph_mode 0 never captures.
+  // Fork/join: the LSM cluster launches run on `side`, concurrently with the
+  // Monte Carlo groups on `stream`, so each fills the other's tail.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int graph_mode = 1;
   long long launches_done = 0;
   bool graph_failed = false;
