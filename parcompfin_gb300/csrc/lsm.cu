@@ -826,6 +826,86 @@ bool coop_shape(const pcf_ctx* c, const LsmLimits& Lm, long long H, int M, int& 
   return lsm_fits(Lm, PB, M, 2, Lm.stat_coop, 1);
 }
 
+// A grid of whole clusters for the two-level exchange
+// (lsm_coop_cluster_kernel) of one contract of H pairs whose plain
+// cooperative grid is G blocks of `smem` bytes: as many clusters of 8 (else 4)
+// CTAs as the device co-schedules, which cluster placement can make fewer
+// than the SMs. hcl = 0 when the plain cooperative kernel should run. Measured
+// on one put, 50 dates: 2^19 paths 0.40 -> 0.33 ms, 2^20 0.46 -> 0.39, 2^21
+// 0.62 -> 0.53.
+void hybrid_shape(const LsmLimits& Lm, long long H, int M, int G, size_t smem, int& hcl, int& Gh,
+                  int& PBh) {
+  hcl = Gh = PBh = 0;
+  for (int cl : {8, 4}) {
+    if (G < 2 * cl) continue;
+    cudaLaunchConfig_t q = {};
+    cudaLaunchAttribute qa[1];
+    qa[0].id = cudaLaunchAttributeClusterDimension;
+    qa[0].val.clusterDim.x = cl;
+    qa[0].val.clusterDim.y = 1;
+    qa[0].val.clusterDim.z = 1;
+    q.gridDim = dim3(cl);
+    q.blockDim = dim3(kLsmBlock);
+    q.dynamicSmemBytes = smem;
+    q.attrs = qa;
+    q.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, lsm_coop_cluster_kernel, &q) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    const int g = std::min((G + cl - 1) / cl, ncl) * cl;
+    if (g < 2 * cl || g * 5 < G * 4) continue;  // keep at least 80 % of the grid
+    const int pb = (int)(((H + g - 1) / g + 3) & ~3LL);
+    // Below ~1024 pairs per CTA the in-cluster exchange costs more than the
+    // global barrier it spares (measured: 2^17 paths 0.32 -> 0.38 ms).
+    if (pb < 1024 || !lsm_fits(Lm, pb, M, 2, Lm.stat_coop, 1)) continue;
+    hcl = cl;
+    Gh = g;
+    PBh = pb;
+    break;
+  }
+}
+
+// Launches one contract's sweep on the hybrid grid if hcl > 0, else (or if
+// the device refuses that launch) on the plain cooperative grid.
+int launch_coop(const LsmParams& P0, int G, int PB, size_t smem, int hcl, int Gh, int PBh,
+                cudaStream_t s, bool* used_hybrid) {
+  LsmParams P = P0;
+  *used_hybrid = false;
+  if (hcl > 0) {
+    P.pairs_per_block = PBh;
+    P.nblocks = Gh;
+    P.cluster = hcl;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = hcl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeCooperative;
+    at[1].val.cooperative = 1;
+    cfg.gridDim = dim3(Gh);
+    cfg.blockDim = dim3(kLsmBlock);
+    cfg.dynamicSmemBytes = lsm_smem(PBh, P.M, 2);
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 2;
+    if (cudaLaunchKernelEx(&cfg, lsm_coop_cluster_kernel, P) == cudaSuccess) {
+      *used_hybrid = true;
+      return PCF_OK;
+    }
+    cudaGetLastError();
+  }
+  P.pairs_per_block = PB;
+  P.nblocks = G;
+  P.cluster = 0;
+  void* args[] = {&P};
+  return cuda_status(cudaLaunchCooperativeKernel((void*)lsm_kernel, dim3(G), dim3(kLsmBlock), args,
+                                                 smem, s),
+                     "lsm cooperative launch");
+}
+
 constexpr int kLsmPB[] = {512, 1024, 2048, 4096, 8192};
 constexpr int kNumPB = 5;
 
@@ -885,7 +965,7 @@ struct LsmCluster {  // one cluster launch: every contract with the same shape
 struct LsmBatch {
   std::vector<LsmCluster> clusters;
   std::vector<LsmParams> coop;  // contracts too large for one cluster
-  std::vector<int> coop_grid;
+  std::vector<int> coop_grid, coop_pb, coop_hcl, coop_gh, coop_pbh;
   std::vector<size_t> coop_smem;
   void* d_mem = nullptr;
   size_t bytes = 0;
@@ -897,7 +977,7 @@ struct LsmLayout {
   std::vector<int> group;  // launch group of each contract, -1: cooperative kernel
   std::vector<std::vector<int>> members;
   std::vector<size_t> o_params, o_dt, o_paths, o_coop;
-  std::vector<int> coop_G, coop_PB;
+  std::vector<int> coop_G, coop_PB, coop_hcl, coop_Gh, coop_PBh;
   std::vector<size_t> coop_sm;
   size_t upload = 0, total = 0;
 };
@@ -938,15 +1018,20 @@ int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
   L.upload = off;
   L.coop_G.assign(n, 0);
   L.coop_PB.assign(n, 0);
+  L.coop_hcl.assign(n, 0);
+  L.coop_Gh.assign(n, 0);
+  L.coop_PBh.assign(n, 0);
   L.coop_sm.assign(n, 0);
   L.o_coop.assign(n, 0);
   for (size_t i = 0; i < n; ++i) {
     if (L.group[i] >= 0) continue;
     if (!coop_shape(c, Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i], L.coop_sm[i]))
       return set_error(PCF_EINVAL, "American request with N = %lld is too large", reqs[i].N);
+    hybrid_shape(Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_sm[i], L.coop_hcl[i],
+                 L.coop_Gh[i], L.coop_PBh[i]);
+    const size_t gm = (size_t)std::max(L.coop_G[i], L.coop_Gh[i]);
     L.o_coop[i] = off;  // partial (2 G 8 float2) | fpartial (G 5 float2) | 2 counters
-    off = a256(off + 8 * (2 * (size_t)L.coop_G[i] * kRegSums + (size_t)L.coop_G[i] * kMoments) +
-               16);
+    off = a256(off + 8 * (2 * gm * kRegSums + gm * kMoments) + 16);
   }
   L.o_paths.assign(n, 0);
   for (size_t i = 0; i < n; ++i) {
@@ -1038,15 +1123,19 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
     fill(i, P);
     P.pairs_per_block = Lo.coop_PB[i];
     P.nblocks = Lo.coop_G[i];
+    const size_t gm = (size_t)std::max(Lo.coop_G[i], Lo.coop_Gh[i]);
     char* base = d + Lo.o_coop[i];
     P.partial = (double*)base;
-    P.fpartial = (double*)(base + 8 * 2 * (size_t)Lo.coop_G[i] * kRegSums);
-    unsigned* cnt = (unsigned*)(base + 8 * (2 * (size_t)Lo.coop_G[i] * kRegSums +
-                                            (size_t)Lo.coop_G[i] * kMoments));
+    P.fpartial = (double*)(base + 8 * 2 * gm * kRegSums);
+    unsigned* cnt = (unsigned*)(base + 8 * (2 * gm * kRegSums + gm * kMoments));
     P.barrier = cnt;
     P.ticket = cnt + 1;
     B->coop.push_back(P);
     B->coop_grid.push_back(Lo.coop_G[i]);
+    B->coop_pb.push_back(Lo.coop_PB[i]);
+    B->coop_hcl.push_back(Lo.coop_hcl[i]);
+    B->coop_gh.push_back(Lo.coop_Gh[i]);
+    B->coop_pbh.push_back(Lo.coop_PBh[i]);
     B->coop_smem.push_back(Lo.coop_sm[i]);
   }
   st = cuda_status(cudaMemcpyAsync(d, h, Lo.upload, cudaMemcpyHostToDevice, s), "H2D LSM batch");
@@ -1095,10 +1184,9 @@ int lsm_batch_launch_coop(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
     LsmParams& P = B->coop[i];
     st = cuda_status(cudaMemsetAsync(P.barrier, 0, 2 * sizeof(unsigned), s), "memset LSM counters");
     if (st) return st;
-    void* args[] = {&P};
-    st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_kernel, dim3(B->coop_grid[i]),
-                                                 dim3(kLsmBlock), args, B->coop_smem[i], s),
-                     "lsm cooperative launch");
+    bool used = false;
+    st = launch_coop(P, B->coop_grid[i], B->coop_pb[i], B->coop_smem[i], B->coop_hcl[i],
+                     B->coop_gh[i], B->coop_pbh[i], s, &used);
     if (st) return st;
     c->launches += 1;
   }
@@ -1139,42 +1227,8 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if ((long long)occ * c->sm_count < G)
     return set_error(PCF_EINVAL, "LSM grid of %d blocks cannot be co-resident", G);
 
-  // A grid of whole clusters for the two-level exchange
-  // (lsm_coop_cluster_kernel): as many clusters of 8 (else 4) CTAs as the
-  // device co-schedules, which cluster placement can make fewer than the
-  // SMs. The plain cooperative kernel is the fallback. Measured on one put,
-  // 50 dates: 2^19 paths 0.40 -> 0.33 ms, 2^20 0.46 -> 0.39, 2^21 0.62 -> 0.53.
   int hcl = 0, Gh = 0, PBh = 0;
-  for (int cl : {8, 4}) {
-    if (G < 2 * cl) continue;
-    cudaLaunchConfig_t q = {};
-    cudaLaunchAttribute qa[1];
-    qa[0].id = cudaLaunchAttributeClusterDimension;
-    qa[0].val.clusterDim.x = cl;
-    qa[0].val.clusterDim.y = 1;
-    qa[0].val.clusterDim.z = 1;
-    q.gridDim = dim3(cl);
-    q.blockDim = dim3(kLsmBlock);
-    q.dynamicSmemBytes = smem;
-    q.attrs = qa;
-    q.numAttrs = 1;
-    int ncl = 0;
-    if (cudaOccupancyMaxActiveClusters(&ncl, lsm_coop_cluster_kernel, &q) != cudaSuccess) {
-      cudaGetLastError();
-      continue;
-    }
-    const int g = std::min((G + cl - 1) / cl, ncl) * cl;
-    if (g < 2 * cl || g * 5 < G * 4) continue;  // keep at least 80 % of the grid
-    const int pb = (int)((((N / 2) + g - 1) / g + 3) & ~3LL);
-    // Below ~1024 pairs per CTA the in-cluster exchange costs more than the
-    // global barrier it spares (measured: 2^17 paths 0.32 -> 0.38 ms).
-    if (pb < 1024 || !lsm_fits(Lm, pb, M, 2, Lm.stat_coop, 1)) continue;
-    hcl = cl;
-    Gh = g;
-    PBh = pb;
-    break;
-  }
-  bool hybrid = hcl > 0;
+  hybrid_shape(Lm, N / 2, M, G, smem, hcl, Gh, PBh);
   const int Gmax = std::max(G, Gh);
 
   LsmParams P;
@@ -1221,39 +1275,9 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   P.err = (int*)(cnt + 2);
   P.singular = (int*)(cnt + 3);
   P.out = (double*)(d + o_out);
-  if (hybrid) {
-    P.pairs_per_block = PBh;
-    P.nblocks = Gh;
-    P.cluster = hcl;
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[2];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = hcl;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    at[1].id = cudaLaunchAttributeCooperative;
-    at[1].val.cooperative = 1;
-    cfg.gridDim = dim3(Gh);
-    cfg.blockDim = dim3(kLsmBlock);
-    cfg.dynamicSmemBytes = lsm_smem(PBh, M, 2);
-    cfg.stream = c->stream;
-    cfg.attrs = at;
-    cfg.numAttrs = 2;
-    if (cudaLaunchKernelEx(&cfg, lsm_coop_cluster_kernel, P) != cudaSuccess) {
-      cudaGetLastError();
-      hybrid = false;
-      P.pairs_per_block = PB;
-      P.nblocks = G;
-      P.cluster = 0;
-    }
-  }
-  if (!hybrid) {
-    void* args[] = {&P};
-    st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_kernel, dim3(G), dim3(kLsmBlock),
-                                                 args, smem, c->stream),
-                     "lsm kernel launch");
-    if (st) return st;
-  }
+  bool used = false;
+  st = launch_coop(P, G, PB, smem, hcl, Gh, PBh, c->stream, &used);
+  if (st) return st;
   c->launches += 1;
   st = cuda_status(cudaMemcpyAsync(h + o_cnt, d + o_cnt, o_out - o_cnt + sizeof(double) * kMoments,
                                    cudaMemcpyDeviceToHost, c->stream),
