@@ -104,40 +104,59 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
 // g = payoff of the geometric mean exp(sum_m w_m log S_m): mode 0 uses the
 // trapezoid weights (w_M = 1/(2M), S_0's weight multiplies log S0/S0 = 0),
 // mode 1 equal weights 1/M on S_1..S_M.
+// One monitoring step of an Asian path (see asia_item).
+template <int MODE, bool CV>
+__device__ __forceinline__ void asia_step(const McContract& C, float w, float z, float& L,
+                                          float& I, float& lg) {
+  if (MODE == 0) {
+    const float S = C.S0 * ex2_approx(L);
+    I = fmaf(S, fmaf(C.c2, z, C.c1), I);
+    L += fmaf(C.b2, z, C.a2);
+  } else {
+    L += fmaf(C.b2, z, C.a2);
+    I += C.S0 * ex2_approx(L);
+  }
+  if (CV) lg = fmaf(w, L, lg);
+}
+
+// One Asian path: the full groups of four steps (one Philox block each) run
+// without per-step checks; the last 1..3 steps, if any, follow.
+template <int MODE, bool CV>
+__device__ __forceinline__ void asia_path(const McContract& C, const RngKey& key, long long n,
+                                          float w, Moments<CV>& mo) {
+  const int M = C.M, Mfull = M & ~3;
+  float L = 0.f, I = 0.f, lg = 0.f;
+  for (int m0 = 0; m0 < Mfull; m0 += 4) {
+    const float4 z = normals4(draw_words(key, (uint64_t)n, (uint32_t)(m0 >> 2)));
+    asia_step<MODE, CV>(C, w, z.x, L, I, lg);
+    asia_step<MODE, CV>(C, w, z.y, L, I, lg);
+    asia_step<MODE, CV>(C, w, z.z, L, I, lg);
+    asia_step<MODE, CV>(C, w, z.w, L, I, lg);
+  }
+  if (Mfull < M) {
+    const float4 z = normals4(draw_words(key, (uint64_t)n, (uint32_t)(Mfull >> 2)));
+    asia_step<MODE, CV>(C, w, z.x, L, I, lg);
+    if (Mfull + 1 < M) asia_step<MODE, CV>(C, w, z.y, L, I, lg);
+    if (Mfull + 2 < M) asia_step<MODE, CV>(C, w, z.z, L, I, lg);
+  }
+  // Mode 0's trapezoid weight on the last level is w_last, not w.
+  if (CV && MODE == 0) lg = fmaf(C.w_last - w, L, lg);
+  const float Y = payoff(C, I * w);
+  const float G = CV ? payoff(C, C.S0 * ex2_approx(lg)) : 0.f;
+  mo.add(Y, G);
+}
+
 template <bool CV>
 __device__ __forceinline__ void asia_item(const McContract& C, int j, Moments<CV>& mo) {
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_ASIA};
-  const int M = C.M;
-  const float w = 1.f / (float)M;
+  const float w = 1.f / (float)C.M;
   const int ppt = C.units_per_item / kBlock;
 #pragma unroll 1
   for (int k = 0; k < ppt; ++k) {
     const long long n = (long long)j * C.units_per_item + (long long)k * kBlock + threadIdx.x;
     if (n >= C.N) break;
-    float L = 0.f, I = 0.f, lg = 0.f;
-    for (int m0 = 0; m0 < M; m0 += 4) {
-      const float4 z = normals4(draw_words(key, (uint64_t)n, (uint32_t)(m0 >> 2)));
-#pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        const int m = m0 + l;
-        if (m < M) {
-          const float zl = lane4(z, l);
-          if (C.mode == 0) {
-            const float S = C.S0 * ex2_approx(L);
-            I = fmaf(S, fmaf(C.c2, zl, C.c1), I);
-            L += fmaf(C.b2, zl, C.a2);
-            if (CV) lg = fmaf(m == M - 1 ? C.w_last : w, L, lg);
-          } else {
-            L += fmaf(C.b2, zl, C.a2);
-            I += C.S0 * ex2_approx(L);
-            if (CV) lg = fmaf(w, L, lg);
-          }
-        }
-      }
-    }
-    const float Y = payoff(C, I * w);
-    const float G = CV ? payoff(C, C.S0 * ex2_approx(lg)) : 0.f;
-    mo.add(Y, G);
+    if (C.mode == 0) asia_path<0, CV>(C, key, n, w, mo);
+    else asia_path<1, CV>(C, key, n, w, mo);
   }
 }
 
@@ -562,17 +581,15 @@ __global__ void __launch_bounds__(kTcBlock, 4) mc_basket_tc_kernel(McLaunch L) {
 }
 
 // Dynamic shared memory above 48 KB and the largest shared-memory carveout,
-// so that four CTAs share an SM.
+// so that four CTAs share an SM. Function attributes belong to the current
+// device, so they are set on every launch (two host calls, no device work).
 template <int DMAX, bool CV>
 void tc_setup() {
-  static bool done = false;
-  if (done) return;
   cudaFuncSetAttribute(mc_basket_tc_kernel<DMAX, CV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tc_basket_smem<DMAX>());
   cudaFuncSetAttribute(mc_basket_tc_kernel<DMAX, CV>,
                        cudaFuncAttributePreferredSharedMemoryCarveout,
                        (int)cudaSharedmemCarveoutMaxShared);
-  done = true;
 }
 
 template <int DMAX, bool CV>
