@@ -452,21 +452,30 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
     const long long p = p0 + i;
     float Lp = 0.f, Lm = 0.f, Sp = 0.f, Sm = 0.f;
     float* row = P.paths + p;
-    for (int m0 = 0; m0 < M; m0 += 4) {
+    // Date m0 + l + 1 takes lane l of Philox block m0 / 4: whole blocks first,
+    // without per-date checks, then the last 1..3 dates.
+    auto step = [&](float z) {
+      Lp += fmaf(P.b2, z, P.a2);
+      Lm += fmaf(nb2, z, P.a2);
+      Sp = ex2_approx(P.l2S0 + Lp);
+      Sm = ex2_approx(P.l2S0 + Lm);
+      row[0] = Sp;
+      row[P.Hp] = Sm;
+      row += stride;
+    };
+    const int Mfull = M & ~3;
+    for (int m0 = 0; m0 < Mfull; m0 += 4) {
       const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(m0 >> 2)));
-      const float zz[4] = {z4.x, z4.y, z4.z, z4.w};
-#pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        if (m0 + l < M) {  // date m0 + l + 1 takes lane l
-          Lp += fmaf(P.b2, zz[l], P.a2);
-          Lm += fmaf(nb2, zz[l], P.a2);
-          Sp = ex2_approx(P.l2S0 + Lp);
-          Sm = ex2_approx(P.l2S0 + Lm);
-          row[0] = Sp;
-          row[P.Hp] = Sm;
-          row += stride;
-        }
-      }
+      step(z4.x);
+      step(z4.y);
+      step(z4.z);
+      step(z4.w);
+    }
+    if (Mfull < M) {
+      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(Mfull >> 2)));
+      step(z4.x);
+      if (Mfull + 1 < M) step(z4.y);
+      if (Mfull + 2 < M) step(z4.z);
     }
     S.cf[i] = lsm_payoff(P, Sp) * dM;
     S.cf[PB + i] = lsm_payoff(P, Sm) * dM;
