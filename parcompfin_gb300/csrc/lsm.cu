@@ -17,15 +17,17 @@
 //                every peer's shared memory and signal the peer's mbarrier.
 // Phases:
 //   forward   each thread generates its antithetic pairs (path p takes +z,
-//             path p + H takes -z, as pathsfinder pairs them) and writes
-//             S(date m), m = 1..M, to an FP32 time-major path matrix in HBM
+//             path p + H takes -z, as pathsfinder pairs them) and writes the
+//             signed moneyness u(date m) = pf (S/E - 1), m = 1..M, to an FP32
+//             time-major path matrix in HBM
 //             (row m-1; plus half at columns [0, Hp), minus half at
 //             [Hp, 2Hp), Hp = H rounded up to 4), coalesced across the warp;
 //   backward  for m = M-1..1 the block's slice of row m-1 (two contiguous
 //             runs) arrives in shared memory by TMA bulk copy, issued two
 //             dates ahead. Each thread updates the exercise decision of its
 //             paths at date m and, in the same pass, adds date m-1's
-//             regression sums in FP32. A warp reduce-scatter leaves the
+//             regression sums in FP32, four consecutive paths per 16-byte
+//             shared-memory load. A warp reduce-scatter leaves the
 //             warp's eight sums in eight lanes; after one block barrier a
 //             single warp adds the warp partials and then all CTAs' partials
 //             in double-float, in a fixed order (every CTA gets the same
@@ -38,8 +40,10 @@
 // Per-path state stays in shared memory for the whole sweep: the cash flow
 // discounted to time 0 (so a date's regression target is one multiply by the
 // date's growth factor) and the exercise date (8 bits where M <= 255). The
-// regression basis is {1, x, x^2} with x = (S - E)/E: the reference's S - E
-// rescaled, the same fitted values in exact arithmetic.
+// regression basis is {1, u, u^2} with u = pf (S - E)/E: the reference's S - E
+// rescaled (and negated for a put), the same fitted values in exact
+// arithmetic. With u stored, a path is in the money where u > 0 and its
+// payoff is E u.
 #include <math.h>
 #include <string.h>
 
@@ -61,7 +65,7 @@ namespace {
 
 constexpr int kLsmBlock = 512;     // cooperative kernel: one block per SM
 constexpr int kLsmCBlock = 512;    // cluster kernel: two CTAs per SM
-constexpr int kRegSums = 8;      // n, x, x^2, x^3, x^4, y, y x, y x^2
+constexpr int kRegSums = 8;      // n, u, u^2, u^3, u^4, y, y u, y u^2
 constexpr int kMaxCluster = 16;  // CTAs per contract in a cluster launch
 
 // How the CTAs of one contract exchange their per-date sums.
@@ -72,8 +76,8 @@ enum LsmMode : int {
 };
 
 struct LsmParams {
-  float pf, nK, E, invE;  // payoff = max(pf S + nK, 0); x = (S - E) * invE
-  float a2, b2, l2S0;     // per-date log2 drift / vol, log2 S0
+  float pf, nK, E, invE;  // payoff = max(pf S + nK, 0) = E max(u, 0)
+  float a2, b2, l2SE;     // per-date log2 drift / vol, log2(S0 / E)
   float rf, sigf, dtf;    // r, sigma, T/M: the European price of the control variate
   int M, ref_exercise;
   long long H;            // antithetic pairs = N / 2
@@ -95,9 +99,9 @@ struct LsmParams {
   double* out;            // kMoments sums
 };
 
-__device__ __forceinline__ float lsm_payoff(const LsmParams& P, float S) {
-  return fmaxf(fmaf(P.pf, S, P.nK), 0.f);
-}
+// Four consecutive floats of shared memory (16-byte aligned).
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
 __device__ __forceinline__ float norm_cdf_f(float x) { return 0.5f * erfcf(-x * 0.70710678f); }
 
@@ -177,12 +181,13 @@ __device__ __forceinline__ void issue_row(const LsmParams& P, int r, long long p
 
 // Adds one path's terms to the regression sums of a date if the path is in
 // the money there (src/mc_amer.cpp:57-66 regresses on in-the-money paths
-// only): x = (S - E)/E and the discounted cash flow y = cfd * growth. Paths
-// out of the money add zeros, so the loop has no divergent branch.
-__device__ __forceinline__ void reg_accumulate(const LsmParams& P, float Sv, float cfd,
-                                               float growth, float (&acc)[kRegSums]) {
-  const bool itm = fmaf(P.pf, Sv, P.nK) > 0.f;
-  const float x = itm ? (Sv - P.E) * P.invE : 0.f;
+// only): u = pf (S - E)/E and the discounted cash flow y = cfd * growth.
+// Paths out of the money (u <= 0) add zeros, so the loop has no divergent
+// branch.
+__device__ __forceinline__ void reg_accumulate(float u, float cfd, float growth,
+                                               float (&acc)[kRegSums]) {
+  const bool itm = u > 0.f;
+  const float x = itm ? u : 0.f;
   const float y = itm ? cfd * growth : 0.f;
   const float x2 = x * x;
   acc[0] += itm ? 1.f : 0.f;
@@ -347,7 +352,7 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
   g = df_add(g, shfl_xor_df(g, 16));  // lanes 0..7: the contract's sum q = lane
   // include/common.h:98-141 solves the normal equations by the adjugate over
   // the determinant, then a mat-vec product. The normal matrix of the basis
-  // {1, x, x^2} is the symmetric Hankel matrix [[a0,a1,a2],[a1,a2,a3],
+  // {1, u, u^2} is the symmetric Hankel matrix [[a0,a1,a2],[a1,a2,a3],
   // [a2,a3,a4]], so its adjugate has six distinct cofactors:
   //   c00 = a2 a4 - a3 a3   c01 = a2 a3 - a1 a4   c02 = a1 a3 - a2 a2
   //   c11 = a0 a4 - a2 a2   c12 = a1 a2 - a0 a3   c22 = a0 a2 - a1 a1
@@ -427,6 +432,7 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
   const long long p0 = (long long)b * PB;
   const int nb = (int)max(0LL, min((long long)PB, P.H - p0));  // pairs in this block
   const int nbr = (nb + 3) & ~3;                                // bulk-copy width
+  const int nq = nbr >> 2;                                      // four-path groups
   for (int k = threadIdx.x; k <= M; k += BS) {
     S.dt[k] = P.dtab[k];
     S.edt[k] = P.dtab[M + 1 + k];
@@ -444,23 +450,23 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
 
   // ---- forward: generate and store paths ----
   const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
-  const float dM = P.dtab[M];
+  const float EdM = P.E * P.dtab[M];  // payoff at T = E max(u, 0), discounted
   const size_t stride = (size_t)2 * P.Hp;  // floats per row
   const float nb2 = -P.b2;
 #pragma unroll 2
   for (int i = threadIdx.x; i < nb; i += BS) {
     const long long p = p0 + i;
-    float Lp = 0.f, Lm = 0.f, Sp = 0.f, Sm = 0.f;
+    float Lp = 0.f, Lm = 0.f, Up = 0.f, Um = 0.f;
     float* row = P.paths + p;
     // Date m0 + l + 1 takes lane l of Philox block m0 / 4: whole blocks first,
     // without per-date checks, then the last 1..3 dates.
     auto step = [&](float z) {
       Lp += fmaf(P.b2, z, P.a2);
       Lm += fmaf(nb2, z, P.a2);
-      Sp = ex2_approx(P.l2S0 + Lp);
-      Sm = ex2_approx(P.l2S0 + Lm);
-      row[0] = Sp;
-      row[P.Hp] = Sm;
+      Up = fmaf(P.pf, ex2_approx(P.l2SE + Lp), -P.pf);  // pf (S/E - 1)
+      Um = fmaf(P.pf, ex2_approx(P.l2SE + Lm), -P.pf);
+      row[0] = Up;
+      row[P.Hp] = Um;
       row += stride;
     };
     const int Mfull = M & ~3;
@@ -477,10 +483,21 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
       if (Mfull + 1 < M) step(z4.y);
       if (Mfull + 2 < M) step(z4.z);
     }
-    S.cf[i] = lsm_payoff(P, Sp) * dM;
-    S.cf[PB + i] = lsm_payoff(P, Sm) * dM;
+    S.cf[i] = fmaxf(Up, 0.f) * EdM;
+    S.cf[PB + i] = fmaxf(Um, 0.f) * EdM;
     S.tau[i] = (TauT)M;
     S.tau[PB + i] = (TauT)M;
+  }
+  // Columns [nb, nbr) pad the last block's bulk copies to 16 bytes: u = 0 and
+  // cf = 0 there, so the four-path steps below see paths out of the money
+  // that never exercise and add nothing.
+  for (int i = nb + threadIdx.x; i < nbr; i += BS) {
+    for (int m = 0; m < M; ++m) {
+      P.paths[(size_t)m * stride + p0 + i] = 0.f;
+      P.paths[(size_t)m * stride + P.Hp + p0 + i] = 0.f;
+    }
+    S.cf[i] = 0.f;
+    S.cf[PB + i] = 0.f;
   }
   // The bulk copies below read what this block's threads just stored; the
   // cluster barrier also publishes the exchange mbarriers to the peers.
@@ -532,11 +549,15 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
     const float* sl = S.slice(0);
     const float e1 = S.edt[M - 1];
-    for (int i = threadIdx.x; i < nb; i += BS) {
+    for (int j = threadIdx.x; j < nq; j += BS) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int s = h * PB + i;
-        reg_accumulate(P, sl[s], S.cf[s], e1, acc);
+        const int s = h * PB + 4 * j;
+        const float4 u = ld4(sl + s), c = ld4(S.cf + s);
+        reg_accumulate(u.x, c.x, e1, acc);
+        reg_accumulate(u.y, c.y, e1, acc);
+        reg_accumulate(u.z, c.z, e1, acc);
+        reg_accumulate(u.w, c.w, e1, acc);
       }
     }
     regress(acc, M - 1, -1, 0);
@@ -556,32 +577,45 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
     float acc[kRegSums];
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
+    // Exercise decision at date m (src/mc_amer.cpp:73-106) for one path:
+    // exercise where the path is in the money and the payoff beats the
+    // continuation value; the cash flow becomes the payoff discounted to 0.
+    auto decide = [&](float u, float& cfd, int s) {
+      float cont, ex = u * P.E;  // the payoff before its max with 0
+      if (mode == 1) {
+        cont = cfd * em;
+      } else {
+        cont = fmaf(fmaf(c2, u, c1), u, c0);
+        // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E),
+        // max(pf (S - 2E), 0) = max(E u - pf E, 0).
+        if (P.ref_exercise) ex = fmaxf(fmaf(P.E, u, P.nK), 0.f);
+      }
+      if (u > 0.f && ex > cont) {
+        cfd = ex * dm;
+        S.tau[s] = (TauT)m;
+      }
+    };
 #pragma unroll 2
-    for (int i = threadIdx.x; i < nb; i += BS) {
+    for (int j = threadIdx.x; j < nq; j += BS) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int s = h * PB + i;
-        float cfd = S.cf[s];
-        // Exercise decision at date m (src/mc_amer.cpp:73-106).
+        const int s = h * PB + 4 * j;
+        float4 c = ld4(S.cf + s);
         if (mode != 0) {
-          const float Sv = cur[s];
-          const float v = fmaf(P.pf, Sv, P.nK);  // the payoff before its max with 0
-          float cont, ex = v;
-          if (mode == 1) {
-            cont = cfd * em;
-          } else {
-            const float x = (Sv - P.E) * P.invE;
-            cont = fmaf(fmaf(c2, x, c1), x, c0);
-            // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E).
-            if (P.ref_exercise) ex = fmaxf(P.pf * (Sv - 2.f * P.E), 0.f);
-          }
-          if (v > 0.f && ex > cont) {
-            cfd = ex * dm;
-            S.cf[s] = cfd;
-            S.tau[s] = (TauT)m;
-          }
+          const float4 u = ld4(cur + s);
+          decide(u.x, c.x, s);
+          decide(u.y, c.y, s + 1);
+          decide(u.z, c.z, s + 2);
+          decide(u.w, c.w, s + 3);
+          st4(S.cf + s, c);
         }
-        if (has_next) reg_accumulate(P, nxt[s], cfd, e1, acc);
+        if (has_next) {
+          const float4 u = ld4(nxt + s);
+          reg_accumulate(u.x, c.x, e1, acc);
+          reg_accumulate(u.y, c.y, e1, acc);
+          reg_accumulate(u.z, c.z, e1, acc);
+          reg_accumulate(u.w, c.w, e1, acc);
+        }
       }
     }
     if (!has_next) break;
@@ -619,7 +653,7 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
       if (P.ref_exercise) {
         // The reference's exercise value does not identify S_tau: use the
         // discounted European payoff at T (mean: the same P_E(S0, T)).
-        g = S.dt[M] * lsm_payoff(P, last[h * P.Hp + p0 + i]);
+        g = S.dt[M] * (P.E * fmaxf(last[h * P.Hp + p0 + i], 0.f));
       } else if (tau == M) {
         g = cfd;  // the discounted European payoff at T
       } else {
@@ -704,7 +738,7 @@ void lsm_fill(LsmParams& P, double S0, double E, double r, double sigma, double 
   P.invE = (float)(1.0 / E);
   P.a2 = (float)((r - 0.5 * sigma * sigma) * dtd * log2e);
   P.b2 = (float)(sigma * sqrt(dtd) * log2e);
-  P.l2S0 = (float)(log(S0) * log2e);
+  P.l2SE = (float)(log(S0 / E) * log2e);
   P.rf = (float)r;
   P.sigf = (float)sigma;
   P.dtf = (float)dtd;
