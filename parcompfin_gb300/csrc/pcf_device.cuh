@@ -76,17 +76,23 @@ __device__ __forceinline__ float cos_approx(float x) {
   return y;
 }
 
+// The Box-Muller angle pi (2 u - 1) of u = uniform_open(w) in one FMA:
+// f = 2 + (w >> 9) 2^-22 (exact, in [2, 4)) and pi (2 u - 1) = pi f - 3 pi +
+// pi 2^-23 in exact arithmetic.
+__device__ __forceinline__ float bm_angle(uint32_t w) {
+  const float f = __uint_as_float(0x40000000u | (w >> 9));
+  return fmaf(3.14159265359f, f, -9.42477758f);  // -3 pi + pi 2^-23, rounded
+}
+
 // Box-Muller on two uniform pairs: (z0,z1) from (w0,w1), (z2,z3) from (w2,w3).
 // z = sqrt(-2 ln u0) * (cos, sin)(pi * (2 u1 - 1)).
 __device__ __forceinline__ float4 normals4(uint4 w) {
   const float kNeg2Ln2 = -1.38629436112f;  // -2 ln 2: -2 ln u = -2 ln2 * log2 u
-  const float kPi = 3.14159265359f;
-  const float u0 = uniform_open(w.x), u1 = uniform_open(w.y);
-  const float u2 = uniform_open(w.z), u3 = uniform_open(w.w);
+  const float u0 = uniform_open(w.x), u2 = uniform_open(w.z);
   const float r0 = sqrt_approx(kNeg2Ln2 * lg2_approx(u0));
   const float r1 = sqrt_approx(kNeg2Ln2 * lg2_approx(u2));
-  const float t0 = kPi * fmaf(2.f, u1, -1.f);
-  const float t1 = kPi * fmaf(2.f, u3, -1.f);
+  const float t0 = bm_angle(w.y);
+  const float t1 = bm_angle(w.w);
   return make_float4(r0 * cos_approx(t0), r0 * sin_approx(t0), r1 * cos_approx(t1),
                      r1 * sin_approx(t1));
 }
