@@ -347,6 +347,7 @@ int pcf_ctx_destroy(pcf_ctx* c) {
   if (!c) return PCF_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  serve_release(c);
   ctx_release_extras(c);
   if (c->d_buf) cudaFree(c->d_buf);
   if (c->h_buf) cudaFreeHost(c->h_buf);

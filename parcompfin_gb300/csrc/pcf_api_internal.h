@@ -5,6 +5,7 @@
 #include <stdarg.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/pcf.h"
@@ -27,6 +28,8 @@ struct pcf_ctx {
   double* d_logtab = nullptr;  // one allocation: log table, prefix tables, ties
   int logtab_n = 0;
   size_t binom_off[4] = {0, 0, 0, 0};  // offsets of prefix sums, tie offsets, ties, stirlerr
+  // Serving slots of pcf_serve_trace, kept between calls (pcf_server.cpp).
+  void* serve = nullptr;
   // Upper bound on device bytes this context may hold (0 = unlimited).
   size_t budget_bytes = 0;
   long long launches = 0;
@@ -39,6 +42,7 @@ int cuda_status(cudaError_t e, const char* what);
 int ctx_ensure(pcf_ctx* c, size_t dev_bytes, size_t host_bytes);
 pcf_ctx* resolve_ctx(pcf_ctx* ctx, int* status);
 void ctx_release_extras(pcf_ctx* c);
+void serve_release(pcf_ctx* c);  // frees the serving slots (pcf_server.cpp)
 int check_common(double S0, double E, double r, double sigma, double T, long long N, int pf);
 void fill_result(const double* s, long long n, double mu_g, double disc, bool use_cv,
                  pcf_mc_result* out);
@@ -74,20 +78,29 @@ void fill_amer_result(const double* s, long long N, double S0, double E, double 
                       double T, int pf, bool use_cv, pcf_mc_result* out);
 // Caller-provided memory for building a batch without allocating: bump
 // allocation from a device region and a pinned host region (256-byte aligned).
+// A failed allocation records how far the region would have had to reach
+// (d_short / h_short), so a caller that owns the regions can grow them and
+// build again.
 struct ExtMem {
   char* d = nullptr;
-  size_t d_cap = 0, d_used = 0;
+  size_t d_cap = 0, d_used = 0, d_short = 0;
   char* h = nullptr;
-  size_t h_cap = 0, h_used = 0;
+  size_t h_cap = 0, h_used = 0, h_short = 0;
   char* dalloc(size_t n) {
     const size_t o = (d_used + 255) & ~(size_t)255;
-    if (o + n > d_cap) return nullptr;
+    if (o + n > d_cap) {
+      d_short = std::max(d_short, o + n);
+      return nullptr;
+    }
     d_used = o + n;
     return d + o;
   }
   char* halloc(size_t n) {
     const size_t o = (h_used + 255) & ~(size_t)255;
-    if (o + n > h_cap) return nullptr;
+    if (o + n > h_cap) {
+      h_short = std::max(h_short, o + n);
+      return nullptr;
+    }
     h_used = o + n;
     return h + o;
   }

@@ -468,12 +468,41 @@ int pcf_plan_destroy(pcf_plan* p) {
   return PCF_OK;
 }
 
+// The one-shot plan lives in the context's scratch arena (device and pinned
+// host), which grows to the largest batch seen and is kept: after the first
+// call of a given size a batch allocates nothing. A build that does not fit
+// reports how far the arena must reach; the arena grows and the build runs
+// again (at most a few times, only while the arena grows).
 int pcf_price_batch(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_mc_result* results) {
+  if (n < 0 || (n > 0 && (!reqs || !results))) return set_error(PCF_EINVAL, "bad batch arguments");
+  int st;
+  pcf_ctx* c = resolve_ctx(ctx, &st);
+  if (!c) return st;
+  cudaSetDevice(c->device);
+  size_t dneed = std::max(c->d_cap, (size_t)1 << 20), hneed = std::max(c->h_cap, (size_t)1 << 20);
   pcf_plan* p = nullptr;
-  int st = pcf_plan_create(ctx, n, reqs, &p);
+  for (int attempt = 0;; ++attempt) {
+    st = ctx_ensure(c, dneed, hneed);
+    if (st) return st;
+    ExtMem mem;
+    mem.d = (char*)c->d_buf;
+    mem.d_cap = c->d_cap;
+    mem.h = (char*)c->h_buf;
+    mem.h_cap = c->h_cap;
+    st = plan_build(c, n, reqs, c->stream, &mem, &p);
+    if (st != PCF_ENOMEM || (!mem.d_short && !mem.h_short) || attempt == 4) break;
+    // Grow past the shortfall; later parts of the build may need more. A
+    // failed build may have queued its table upload: let it land before the
+    // arena is replaced.
+    cudaStreamSynchronize(c->stream);
+    dneed = std::max(dneed, mem.d_short + mem.d_short / 4);
+    hneed = std::max(hneed, mem.h_short + mem.h_short / 4);
+  }
   if (st) return st;
-  st = pcf_plan_launch(p);
-  if (!st) st = pcf_plan_results(p, results);
+  st = plan_launch(p);
+  if (!st) st = plan_fetch(p);
+  if (!st) st = cuda_status(cudaStreamSynchronize(p->stream), "batch kernels");
+  if (!st) st = plan_fill_results(p, results);
   pcf_plan_destroy(p);
   return st;
 }

@@ -2,15 +2,19 @@
 //
 // The loop owns S slots. Each slot has a CUDA stream, an event, and a device
 // and a pinned host region reserved at start-up (a share of the free HBM), so
-// no allocation happens while serving. A slot runs one batch through:
+// no allocation happens while serving. The slots belong to the context and
+// are kept between calls (a server reserves its memory once, not per trace);
+// pcf_ctx_destroy frees them, and a call asking for another slot count
+// replaces them. A slot runs one batch through:
 //   PILOT  every request at a small path count, to estimate the variance of
 //          its estimator;
 //   MAIN   every request at the path count that reaches its target standard
 //          error, in chunks that fit the slot's memory (American path
 //          matrices dominate it).
 // Between polls the loop admits every request whose arrival time has passed
-// into a free slot (up to max_batch), so work admitted while other slots run
-// overlaps with them on the device. Latency is arrival -> result on the host,
+// into the free slots, spread evenly over them (at most max_batch each), so
+// work admitted while other slots run overlaps with them on the device, and
+// one slot's host-side plan build overlaps another's kernels. Latency is arrival -> result on the host,
 // measured on the wall clock.
 #include <math.h>
 #include <string.h>
@@ -44,6 +48,27 @@ struct Slot {
   pcf_plan* plan = nullptr;
 };
 
+// The slots of a context, kept between pcf_serve_trace calls.
+struct ServeCache {
+  std::vector<Slot> slots;
+  size_t per_slot = 0;
+};
+
+void free_slots(std::vector<Slot>& slots) {
+  for (Slot& s : slots) {
+    if (s.plan) {
+      cudaStreamSynchronize(s.s);
+      pcf_plan_destroy(s.plan);
+      s.plan = nullptr;
+    }
+    if (s.d) cudaFree(s.d);
+    if (s.h) cudaFreeHost(s.h);
+    if (s.ev) cudaEventDestroy(s.ev);
+    if (s.s) cudaStreamDestroy(s.s);
+  }
+  slots.clear();
+}
+
 long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 
 // Device bytes a request's main run needs (American: its path matrix).
@@ -64,7 +89,7 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
   if (cfg.max_paths <= 0) cfg.max_paths = 1LL << 26;
   if (cfg.max_amer_paths <= 0) cfg.max_amer_paths = 1LL << 21;
   if (cfg.max_batch <= 0) cfg.max_batch = 2048;
-  if (cfg.slots <= 0) cfg.slots = 3;
+  if (cfg.slots <= 0) cfg.slots = 4;
   if (cfg.hbm_fraction <= 0 || cfg.hbm_fraction > 0.9) cfg.hbm_fraction = 0.5;
   for (int i = 1; i < n; ++i)
     if (arrival[i] < arrival[i - 1]) return set_error(PCF_EINVAL, "arrival times must not decrease");
@@ -72,42 +97,58 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
   pcf_ctx* c = resolve_ctx(ctx, &st);
   if (!c) return st;
 
-  // Reserve the slots' memory once.
-  size_t free_b = 0, total_b = 0;
-  st = cuda_status(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-  if (st) return st;
-  size_t budget = (size_t)(cfg.hbm_fraction * (double)free_b);
-  if (c->budget_bytes) budget = std::min(budget, c->budget_bytes);
-  // A slot needs at most a few chunks of American path matrices (a 2^21-path,
-  // 50-date contract is 420 MB): 8 GB per slot is ample, and reserving less
-  // keeps start-up short.
-  const size_t per_slot = std::min(budget / cfg.slots, (size_t)8 << 30);
-  const size_t host_per_slot = (size_t)16 << 20;
-  std::vector<Slot> slots(cfg.slots);
+  // Reserve the slots' memory once per context.
+  ServeCache* sc = static_cast<ServeCache*>(c->serve);
+  if (sc && (int)sc->slots.size() != cfg.slots) {
+    serve_release(c);
+    sc = nullptr;
+  }
+  if (!sc) {
+    size_t free_b = 0, total_b = 0;
+    st = cuda_status(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    if (st) return st;
+    size_t budget = (size_t)(cfg.hbm_fraction * (double)free_b);
+    if (c->budget_bytes) budget = std::min(budget, c->budget_bytes);
+    // A slot needs at most a few chunks of American path matrices (a
+    // 2^21-path, 50-date contract is 420 MB): 8 GB per slot is ample, and
+    // reserving less keeps start-up short.
+    const size_t per_slot = std::min(budget / cfg.slots, (size_t)8 << 30);
+    const size_t host_per_slot = (size_t)16 << 20;
+    sc = new ServeCache;
+    sc->slots.resize(cfg.slots);
+    sc->per_slot = per_slot;
+    for (Slot& s : sc->slots) {
+      st = cuda_status(cudaStreamCreateWithFlags(&s.s, cudaStreamNonBlocking), "slot stream");
+      if (!st)
+        st = cuda_status(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming), "slot event");
+      if (!st) st = cuda_status(cudaMalloc((void**)&s.d, per_slot), "slot device memory");
+      if (!st) st = cuda_status(cudaMallocHost((void**)&s.h, host_per_slot), "slot pinned memory");
+      if (st) {
+        free_slots(sc->slots);
+        delete sc;
+        return st;
+      }
+      s.d_cap = per_slot;
+      s.h_cap = host_per_slot;
+    }
+    c->serve = sc;
+  }
+  std::vector<Slot>& slots = sc->slots;
+  const size_t per_slot = sc->per_slot;
+  // Leaves every slot free for the next call (a failed batch may hold a plan).
   auto release = [&]() {
     for (Slot& s : slots) {
       if (s.plan) {
         cudaStreamSynchronize(s.s);
         pcf_plan_destroy(s.plan);
+        s.plan = nullptr;
       }
-      if (s.d) cudaFree(s.d);
-      if (s.h) cudaFreeHost(s.h);
-      if (s.ev) cudaEventDestroy(s.ev);
-      if (s.s) cudaStreamDestroy(s.s);
+      s.state = Slot::FREE;
+      s.ids.clear();
+      s.main_q.clear();
+      s.pilot_n.clear();
     }
   };
-  for (Slot& s : slots) {
-    st = cuda_status(cudaStreamCreateWithFlags(&s.s, cudaStreamNonBlocking), "slot stream");
-    if (!st) st = cuda_status(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming), "slot event");
-    if (!st) st = cuda_status(cudaMalloc((void**)&s.d, per_slot), "slot device memory");
-    if (!st) st = cuda_status(cudaMallocHost((void**)&s.h, host_per_slot), "slot pinned memory");
-    if (st) {
-      release();
-      return st;
-    }
-    s.d_cap = per_slot;
-    s.h_cap = host_per_slot;
-  }
 
   for (int i = 0; i < n; ++i) {
     memset(&out[i], 0, sizeof out[i]);
@@ -240,16 +281,23 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
         }
       }
     }
-    // Admit arrived requests into free slots.
+    // Admit arrived requests into free slots, an even share each (a burst
+    // of 1000 requests into four free slots runs as four pipelined batches:
+    // measured 6.99 -> 5.24 ms against one batch).
+    int free_slots = 0;
+    for (const Slot& s : slots) free_slots += s.state == Slot::FREE;
     for (Slot& s : slots) {
       if (pending.empty()) break;
       if (s.state != Slot::FREE) continue;
       progress = true;
+      const size_t share = std::min<size_t>(
+          (size_t)cfg.max_batch, (pending.size() + free_slots - 1) / (size_t)free_slots);
+      --free_slots;
       s.ids.clear();
       s.pilot_n.clear();
       std::vector<pcf_mc_request> q;
       const double ta = now();
-      while (!pending.empty() && (int)s.ids.size() < cfg.max_batch) {
+      while (!pending.empty() && s.ids.size() < share) {
         const int id = pending.front();
         pending.pop_front();
         s.ids.push_back(id);
@@ -336,3 +384,15 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
   }
   return failures ? first_error : PCF_OK;
 }
+
+namespace pcf {
+
+void serve_release(pcf_ctx* c) {
+  ServeCache* sc = static_cast<ServeCache*>(c->serve);
+  if (!sc) return;
+  free_slots(sc->slots);
+  delete sc;
+  c->serve = nullptr;
+}
+
+}  // namespace pcf
