@@ -84,7 +84,7 @@ int basket_class(int d) { return d <= 4 ? 0 : d <= 8 ? 1 : d <= 16 ? 2 : d <= 32
 namespace pcf {
 
 int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, ExtMem* mem,
-               pcf_plan** out) {
+               pcf_plan** out, const long long* path0) {
   *out = nullptr;
   pcf_plan* p = new pcf_plan();
   p->ctx = c;
@@ -127,6 +127,13 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
     if (st) {
       delete p;
       return st;
+    }
+    if (path0 && path0[i]) {
+      if (path0[i] < 0 || path0[i] % 4 != 0) {
+        delete p;
+        return set_error(PCF_EINVAL, "request %d: path offset must be a multiple of 4", i);
+      }
+      k.x0 = m == PCF_METHOD_EUR ? path0[i] / 4 : path0[i];
     }
     if (m == PCF_METHOD_BASKET) g[gi].max_d = std::max(g[gi].max_d, reqs[i].assets);
     p->npaths[i] = reqs[i].N;

@@ -31,6 +31,8 @@ struct McContract {
   float nK;              // -pf * K: payoff = max(pf * S + nK, 0)
   float l2S0;            // log2(S0)
   float pad2;
+  long long x0;          // first Philox x coordinate: path quad (European) or path, so a
+                         // contract can continue the paths of an earlier run
 };
 
 // Basket factor block (device): per asset log2(S0_a) + (r - s_a^2/2) T log2e,

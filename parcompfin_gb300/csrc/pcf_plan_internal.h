@@ -59,9 +59,12 @@ namespace pcf {
 
 // Builds a plan on stream s. mem == NULL: owns its memory, uploads
 // synchronously. Otherwise: takes memory from mem (no allocation) and only
-// queues the upload.
+// queues the upload. path0 (optional, one per request): the request's paths
+// are paths [path0, path0 + N) of its stream, so a run can continue an
+// earlier one and the two sets of sums add up (European, Asian and basket;
+// path0 must be a multiple of 4 and is ignored for American requests).
 int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, ExtMem* mem,
-               pcf_plan** out);
+               pcf_plan** out, const long long* path0 = nullptr);
 int plan_launch(pcf_plan* p);
 // Queues the device-to-host copy of the results (no wait).
 int plan_fetch(pcf_plan* p);

@@ -6,11 +6,17 @@
 // are kept between calls (a server reserves its memory once, not per trace);
 // pcf_ctx_destroy frees them, and a call asking for another slot count
 // replaces them. A slot runs one batch through:
-//   PILOT  every request at a small path count, to estimate the variance of
-//          its estimator;
-//   MAIN   every request at the path count that reaches its target standard
-//          error, in chunks that fit the slot's memory (American path
-//          matrices dominate it).
+//   PILOT  every request at a small path count n0, to estimate the variance
+//          of its estimator;
+//   MAIN   every request at the path count N that reaches its target
+//          standard error, in chunks that fit the slot's memory (American
+//          path matrices dominate it). A European, Asian or basket request
+//          continues its pilot: the main run prices paths [n0, N) of the same
+//          stream, and the pilot's sums and the main run's sums add up to the
+//          sums over paths [0, N) (the same paths as one run of N; only the
+//          order of the additions differs). A request whose pilot already
+//          reaches the target is done after the pilot. An American request
+//          runs again at N: its regression needs every path in one sweep.
 // Between polls the loop admits every request whose arrival time has passed
 // into the free slots, spread evenly over them (at most max_batch each), so
 // work admitted while other slots run overlaps with them on the device, and
@@ -43,6 +49,8 @@ struct Slot {
   enum { FREE, PILOT, MAIN } state = FREE;
   std::vector<int> ids;                 // requests of the batch
   std::vector<pcf_mc_request> main_q;   // main-run requests (same order as ids)
+  std::vector<long long> main_x0;       // first path of each main request (0: a fresh run)
+  std::vector<pcf_mc_result> carry;     // the pilot result a main request continues
   std::vector<long long> pilot_n;
   size_t chunk_lo = 0, chunk_hi = 0;    // [lo, hi) of ids in the running main chunk
   pcf_plan* plan = nullptr;
@@ -146,6 +154,8 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
       s.state = Slot::FREE;
       s.ids.clear();
       s.main_q.clear();
+      s.main_x0.clear();
+      s.carry.clear();
       s.pilot_n.clear();
     }
   };
@@ -187,7 +197,8 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
       ++k;
     }
     s.chunk_hi = k;
-    int e = plan_build(c, (int)(s.chunk_hi - s.chunk_lo), &s.main_q[s.chunk_lo], s.s, &mem, &s.plan);
+    int e = plan_build(c, (int)(s.chunk_hi - s.chunk_lo), &s.main_q[s.chunk_lo], s.s, &mem, &s.plan,
+                       &s.main_x0[s.chunk_lo]);
     if (!e) e = plan_launch(s.plan);
     if (!e) e = plan_fetch(s.plan);
     if (!e) e = cuda_status(cudaEventRecord(s.ev, s.s), "slot event record");
@@ -228,8 +239,13 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
       if (s.state == Slot::PILOT) {
         // Path count that reaches the target relative SE, from the pilot.
         s.main_q.clear();
+        s.main_x0.clear();
+        s.carry.clear();
+        std::vector<int> main_ids;
+        const double tp = now();
         for (size_t j = 0; j < s.ids.size(); ++j) {
-          pcf_mc_request q = reqs[s.ids[j]];
+          const int id = s.ids[j];
+          pcf_mc_request q = reqs[id];
           const pcf_mc_result& r = res[j];
           const double se = q.use_cv ? r.std_error_cv : r.std_error_plain;
           const double price = fabs(q.use_cv ? r.price_cv : r.price_plain);
@@ -240,17 +256,34 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
             const double need = (se * se * (double)n0) / (target * target) * 1.05;
             N = (long long)std::min(std::max(need, (double)n0), 9.0e18);
           }
+          paths += n0;
+          out[id].paths = n0;
+          long long x0 = 0;
           if (q.method == PCF_METHOD_AMER) {
             N = std::max(N, 1LL << 16);
             N = std::min(N, cfg.max_amer_paths);
             N = round_up(N, 2);
           } else {
             N = std::min(N, cfg.max_paths);
+            if (N <= n0) {  // the pilot reaches the target
+              out[id].result = r;
+              out[id].done_s = tp;
+              ++done;
+              continue;
+            }
+            x0 = n0;
+            N -= n0;
           }
           q.N = N;
-          paths += n0;
-          out[s.ids[j]].paths = n0;
+          main_ids.push_back(id);
           s.main_q.push_back(q);
+          s.main_x0.push_back(x0);
+          s.carry.push_back(r);
+        }
+        s.ids.swap(main_ids);
+        if (s.ids.empty()) {
+          s.state = Slot::FREE;
+          continue;
         }
         s.chunk_lo = 0;
         s.state = Slot::MAIN;
@@ -260,7 +293,16 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
         const double td = now();
         for (size_t j = s.chunk_lo; j < s.chunk_hi; ++j) {
           const int id = s.ids[j];
-          out[id].result = res[j - s.chunk_lo];
+          const pcf_mc_result& b = res[j - s.chunk_lo];
+          if (s.main_x0[j] > 0) {  // pilot sums + main sums: paths [0, N)
+            const pcf_mc_result& a = s.carry[j];
+            double sum[kMoments];
+            for (int k = 0; k < kMoments; ++k) sum[k] = a.sums[k] + b.sums[k];
+            fill_result(sum, a.n_paths + b.n_paths, a.cv_mean, a.discount,
+                        s.main_q[j].use_cv != 0, &out[id].result);
+          } else {
+            out[id].result = b;
+          }
           out[id].done_s = td;
           out[id].paths += s.main_q[j].N;
           paths += s.main_q[j].N;
@@ -304,9 +346,10 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
         out[id].admit_s = ta;
         pcf_mc_request r = reqs[id];
         if (cfg.target_rel_se > 0) {
-          r.N = r.method == PCF_METHOD_AMER ? std::max(cfg.pilot_paths, 1LL << 14)
-                                            : cfg.pilot_paths;
-          r.N = round_up(r.N, 2);
+          // A multiple of 4: the main run of a European, Asian or basket
+          // request starts at path n0.
+          r.N = r.method == PCF_METHOD_AMER ? round_up(std::max(cfg.pilot_paths, 1LL << 14), 2)
+                                            : round_up(cfg.pilot_paths, 4);
         }
         s.pilot_n.push_back(r.N);
         q.push_back(r);
@@ -326,6 +369,8 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
         s.state = Slot::PILOT;
       } else {
         s.main_q = q;
+        s.main_x0.assign(q.size(), 0);
+        s.carry.assign(q.size(), pcf_mc_result{});
         for (size_t j = 0; j < q.size(); ++j) out[s.ids[j]].paths = 0;
         s.chunk_lo = 0;
         s.state = Slot::MAIN;

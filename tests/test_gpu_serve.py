@@ -3,9 +3,14 @@
   * every request of a timed mixed trace completes, at (about) its target
     relative standard error, unless its path count hit the cap;
   * each served result is the same as pricing that request alone at the same
-    path count (the stated tolerance is exact equality of the moment sums:
-    a request's work items and their reduction do not depend on what else is
-    in its batch);
+    path count. Where one run priced it (American requests, and requests whose
+    pilot reached the target) the tolerance is exact equality of the moment
+    sums: a request's work items and their reduction do not depend on what
+    else is in its batch. A European, Asian or basket request whose main run
+    continued its pilot (paths [n0, N) after paths [0, n0)) has the same
+    paths in two partial sums, grouped differently into per-thread FP32
+    partials: equal to 1e-8 relative (measured ~1e-10; other paths would
+    differ by the Monte Carlo noise, ~1e-3);
   * requests arriving while other batches run are admitted into other slots
     (more than one batch in flight).
 """
@@ -16,6 +21,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TARGET = 5e-4
+PILOT = 1 << 14
 
 
 def _trace(pcf, n, rate, seed):
@@ -59,10 +65,19 @@ def test_served_trace_meets_target_and_matches_alone(ctx):
             # the pilot's variance estimate is itself noisy: allow 35 %
             assert rel < 1.35 * TARGET, (q, rel)
     # Same alone: re-price a sample of requests alone at the served path count.
-    for i in range(0, len(reqs), 12):
+    continued = 0
+    for i in range(0, len(reqs), 6):
         q = dict(reqs[i], N=out[i].result.n_paths)
         alone = pcf.price_batch([q], ctx=ctx)[0]
-        assert list(alone.sums) == list(out[i].result.sums), q
+        if q["method"] == 3 or q["N"] <= PILOT:
+            assert list(alone.sums) == list(out[i].result.sums), q
+        else:
+            continued += 1
+            for a, b in zip(alone.sums, out[i].result.sums):
+                assert abs(a - b) <= 1e-8 * max(abs(a), abs(b)), (q, a, b)
+            assert out[i].paths == q["N"]  # the pilot's paths are part of the estimate
+            assert abs(alone.price - out[i].result.price) <= 1e-8 * abs(alone.price)
+    assert continued > 0
     assert sorted(rels)[len(rels) // 2] < TARGET
 
 
