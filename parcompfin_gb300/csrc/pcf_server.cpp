@@ -15,8 +15,10 @@
 //          stream, and the pilot's sums and the main run's sums add up to the
 //          sums over paths [0, N) (the same paths as one run of N; only the
 //          order of the additions differs). A request whose pilot already
-//          reaches the target is done after the pilot. An American request
-//          runs again at N: its regression needs every path in one sweep.
+//          reaches the target is done after the pilot. An American pilot
+//          runs at the American floor of 2^16 paths, so most American
+//          requests are done after it; the others run again at N (a
+//          regression needs every path in one sweep).
 // Between polls the loop admits every request whose arrival time has passed
 // into the free slots, spread evenly over them (at most max_batch each), so
 // work admitted while other slots run overlaps with them on the device, and
@@ -78,6 +80,10 @@ void free_slots(std::vector<Slot>& slots) {
 }
 
 long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
+
+// Fewest paths an American request runs with a standard-error target: below
+// it the regression's own noise dominates the pilot's variance estimate.
+constexpr long long kAmerFloor = 1LL << 16;
 
 // Device bytes a request's main run needs (American: its path matrix).
 size_t main_bytes(const pcf_mc_request& q) {
@@ -260,17 +266,19 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
           out[id].paths = n0;
           long long x0 = 0;
           if (q.method == PCF_METHOD_AMER) {
-            N = std::max(N, 1LL << 16);
+            N = std::max(N, kAmerFloor);
             N = std::min(N, cfg.max_amer_paths);
             N = round_up(N, 2);
           } else {
             N = std::min(N, cfg.max_paths);
-            if (N <= n0) {  // the pilot reaches the target
-              out[id].result = r;
-              out[id].done_s = tp;
-              ++done;
-              continue;
-            }
+          }
+          if (N <= n0 && std::isfinite(r.price)) {  // the pilot reaches the target
+            out[id].result = r;
+            out[id].done_s = tp;
+            ++done;
+            continue;
+          }
+          if (q.method != PCF_METHOD_AMER) {
             x0 = n0;
             N -= n0;
           }
@@ -347,8 +355,10 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
         pcf_mc_request r = reqs[id];
         if (cfg.target_rel_se > 0) {
           // A multiple of 4: the main run of a European, Asian or basket
-          // request starts at path n0.
-          r.N = r.method == PCF_METHOD_AMER ? round_up(std::max(cfg.pilot_paths, 1LL << 14), 2)
+          // request starts at path n0. An American pilot runs at the
+          // American floor: most American requests need no more, and their
+          // pilot is then their result.
+          r.N = r.method == PCF_METHOD_AMER ? round_up(std::max(cfg.pilot_paths, kAmerFloor), 2)
                                             : round_up(cfg.pilot_paths, 4);
         }
         s.pilot_n.push_back(r.N);
