@@ -97,6 +97,8 @@ struct LsmParams {
   int* err;               // 1: a barrier wait gave up, 2: a bulk copy wait gave up
   int* singular;          // dates whose normal equations had det <= 0
   double* out;            // kMoments sums
+  float* gcf;             // streaming sweep: 2*Hp discounted cash flows (device memory)
+  unsigned short* gtau;   // streaming sweep: 2*Hp exercise dates
 };
 
 // Four consecutive floats of shared memory (16-byte aligned).
@@ -704,6 +706,197 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_coop_cluster_kernel(LsmParam
                                                     (int)cg::this_cluster().block_rank());
 }
 
+// Streaming sweep for a contract whose per-block slice does not fit in
+// shared memory (about 2.8e6 paths and more on 152 SMs): the same algorithm
+// as lsm_body's cooperative form, with the cash flows and exercise dates in
+// device memory (P.gcf, P.gtau, laid out like a path-matrix row) and the
+// path rows read straight from it, four paths per 16-byte load. A date then
+// moves 16 bytes per path (date m and m-1, the cash flow in and out) instead
+// of 4; the sweep stays bandwidth-bound at any N.
+__global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
+  constexpr int BS = kLsmBlock, NW = BS / 32;
+  __shared__ LsmShared<NW> X;
+  extern __shared__ __align__(16) float stab[];  // dt[M+1] | edt[M+1]
+  const int b = blockIdx.x, M = P.M;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float* dt = stab;
+  float* edt = stab + (M + 1);
+  const long long PB = P.pairs_per_block, Hp = P.Hp;
+  const long long p0 = (long long)b * PB;
+  const long long nb = max(0LL, min(PB, P.H - p0));
+  const long long nbr = (nb + 3) & ~3LL;
+  const long long nq = nbr >> 2;
+  for (int k = threadIdx.x; k <= M; k += BS) {
+    dt[k] = P.dtab[k];
+    edt[k] = P.dtab[M + 1 + k];
+  }
+  if (threadIdx.x == 0) X.fail = 0;
+
+  // ---- forward: the whole-path loop of lsm_body ----
+  const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
+  const float EdM = P.E * P.dtab[M];
+  const size_t stride = (size_t)2 * Hp;
+  const float nb2 = -P.b2;
+  for (long long i = threadIdx.x; i < nb; i += BS) {
+    const long long p = p0 + i;
+    float Lp = 0.f, Lm = 0.f, Up = 0.f, Um = 0.f;
+    float* row = P.paths + p;
+    auto step = [&](float z) {
+      Lp += fmaf(P.b2, z, P.a2);
+      Lm += fmaf(nb2, z, P.a2);
+      Up = fmaf(P.pf, ex2_approx(P.l2SE + Lp), -P.pf);
+      Um = fmaf(P.pf, ex2_approx(P.l2SE + Lm), -P.pf);
+      row[0] = Up;
+      row[Hp] = Um;
+      row += stride;
+    };
+    const int Mfull = M & ~3;
+    for (int m0 = 0; m0 < Mfull; m0 += 4) {
+      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(m0 >> 2)));
+      step(z4.x);
+      step(z4.y);
+      step(z4.z);
+      step(z4.w);
+    }
+    if (Mfull < M) {
+      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(Mfull >> 2)));
+      step(z4.x);
+      if (Mfull + 1 < M) step(z4.y);
+      if (Mfull + 2 < M) step(z4.z);
+    }
+    P.gcf[p] = fmaxf(Up, 0.f) * EdM;
+    P.gcf[Hp + p] = fmaxf(Um, 0.f) * EdM;
+    P.gtau[p] = (unsigned short)M;
+    P.gtau[Hp + p] = (unsigned short)M;
+  }
+  for (long long i = nb + threadIdx.x; i < nbr; i += BS) {  // padding: out of the money
+    for (int m = 0; m < M; ++m) {
+      P.paths[(size_t)m * stride + p0 + i] = 0.f;
+      P.paths[(size_t)m * stride + Hp + p0 + i] = 0.f;
+    }
+    P.gcf[p0 + i] = 0.f;
+    P.gcf[Hp + p0 + i] = 0.f;
+  }
+  __syncthreads();  // every path of the block is read below by another thread
+
+  uint32_t xph = 0, xcount = 0;
+  auto regress = [&](const float (&acc)[kRegSums], int d) {
+    const float v = warp_scatter8(acc);
+    if ((lane & 3) == 0) X.wpart[wid][lane >> 2] = v;
+    __syncthreads();
+    if (wid == 0) regress_date<kCoop, NW>(P, X, d, b, 0, xph, xcount);
+    __syncthreads();
+  };
+  {
+    float acc[kRegSums];
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
+    const float* rowd = P.paths + (size_t)(M - 2) * stride + p0;  // date M-1
+    const float e1 = edt[M - 1];
+    for (long long j = threadIdx.x; j < nq; j += BS) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const long long s = h * Hp + 4 * j;
+        const float4 u = __ldcs(reinterpret_cast<const float4*>(rowd + s));
+        const float4 c = *reinterpret_cast<const float4*>(P.gcf + p0 + s);
+        reg_accumulate(u.x, c.x, e1, acc);
+        reg_accumulate(u.y, c.y, e1, acc);
+        reg_accumulate(u.z, c.z, e1, acc);
+        reg_accumulate(u.w, c.w, e1, acc);
+      }
+    }
+    regress(acc, M - 1);
+  }
+  bool failed = X.fail;
+  for (int m = M - 1; m >= 1 && !failed; --m) {
+    const bool has_next = m > 1;
+    const int mode = X.mode;
+    const float c0 = X.coef[0], c1 = X.coef[1], c2 = X.coef[2];
+    const float dm = dt[m], em = edt[m], e1 = edt[m - 1];
+    const float* cur = P.paths + (size_t)(m - 1) * stride + p0;  // date m is row m-1
+    const float* nxt = has_next ? cur - stride : cur;
+    float acc[kRegSums];
+#pragma unroll
+    for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
+    auto decide = [&](float u, float& cfd, long long s) {
+      float cont, ex = u * P.E;
+      if (mode == 1) {
+        cont = cfd * em;
+      } else {
+        cont = fmaf(fmaf(c2, u, c1), u, c0);
+        if (P.ref_exercise) ex = fmaxf(fmaf(P.E, u, P.nK), 0.f);  // src/mc_amer.cpp:100
+      }
+      if (u > 0.f && ex > cont) {
+        cfd = ex * dm;
+        P.gtau[p0 + s] = (unsigned short)m;
+      }
+    };
+#pragma unroll 2
+    for (long long j = threadIdx.x; j < nq; j += BS) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const long long s = h * Hp + 4 * j;
+        float4* cp = reinterpret_cast<float4*>(P.gcf + p0 + s);
+        float4 c = *cp;
+        if (mode != 0) {
+          const float4 u = __ldcs(reinterpret_cast<const float4*>(cur + s));
+          decide(u.x, c.x, s);
+          decide(u.y, c.y, s + 1);
+          decide(u.z, c.z, s + 2);
+          decide(u.w, c.w, s + 3);
+          *cp = c;
+        }
+        if (has_next) {
+          const float4 u = *reinterpret_cast<const float4*>(nxt + s);
+          reg_accumulate(u.x, c.x, e1, acc);
+          reg_accumulate(u.y, c.y, e1, acc);
+          reg_accumulate(u.z, c.z, e1, acc);
+          reg_accumulate(u.w, c.w, e1, acc);
+        }
+      }
+    }
+    if (!has_next) break;
+    regress(acc, m - 1);
+    failed = X.fail;
+  }
+  __syncthreads();
+  if (failed) return;
+
+  // ---- final moments over pair means (as lsm_body) ----
+  const float* last = P.paths + (size_t)(M - 1) * stride;
+  KSum sy, syy, sg, sgg, syg;
+  for (long long i = threadIdx.x; i < nb; i += BS) {
+    float y2 = 0.f, g2 = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long s = h * Hp + p0 + i;
+      const int tau = P.gtau[s];
+      const float cfd = P.gcf[s];
+      y2 += cfd;
+      float g;
+      if (P.ref_exercise) {
+        g = dt[M] * (P.E * fmaxf(last[s], 0.f));
+      } else if (tau == M) {
+        g = cfd;
+      } else {
+        const float St = P.E + P.pf * (cfd * edt[tau]);
+        g = dt[tau] * european_price(P, St, (float)(M - tau) * P.dtf);
+      }
+      g2 += g;
+    }
+    const float y = 0.5f * y2, g = 0.5f * g2;
+    sy.add(y);
+    syy.add(y * y);
+    sg.add(g);
+    sgg.add(g * g);
+    syg.add(y * g);
+  }
+  DF v[kMoments] = {df_of(sy), df_of(syy), df_of(sg), df_of(sgg), df_of(syg)};
+  DF tot[kMoments];
+  block_sum_df<kMoments>(v, X.sh, tot);
+  grid_finalize_df<kMoments>(tot, (float2*)P.fpartial, P.ticket, P.out, P.nblocks, b);
+}
+
 // Many contracts in one launch, one thread-block cluster per contract
 // (cluster size = the contracts' common CTA count). Two CTAs per SM: while
 // one runs its per-date exchange and solve, the other's paths keep the SM
@@ -1261,25 +1454,43 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if (Lm.status) return Lm.status;
   int G = 0, PB = 0;
   size_t smem = 0;
-  if (!coop_shape(c, Lm, N / 2, M, G, PB, smem))
-    return set_error(PCF_EINVAL, "N = %lld is too large for one device sweep", N);
-  int occ = 0;
-  st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_kernel, kLsmBlock, smem),
-                   "occupancy(lsm)");
-  if (st) return st;
-  if ((long long)occ * c->sm_count < G)
-    return set_error(PCF_EINVAL, "LSM grid of %d blocks cannot be co-resident", G);
-
+  // A contract whose per-block slice does not fit in shared memory runs the
+  // streaming sweep (per-path state in device memory), one block per SM.
+  const bool streaming = !coop_shape(c, Lm, N / 2, M, G, PB, smem);
   int hcl = 0, Gh = 0, PBh = 0;
-  hybrid_shape(Lm, N / 2, M, G, smem, hcl, Gh, PBh);
+  if (streaming) {
+    smem = sizeof(float) * 2 * (size_t)(M + 1);
+    int occ = 0;
+    st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_stream_kernel,
+                                                                   kLsmBlock, smem),
+                     "occupancy(lsm stream)");
+    if (st) return st;
+    if (occ < 1) return set_error(PCF_EINVAL, "the streaming LSM block does not fit on an SM");
+    const long long H = N / 2;
+    const long long G0 = std::min((long long)c->sm_count, (H + 3) / 4);
+    PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
+    G = (int)((H + PB - 1) / PB);
+  } else {
+    int occ = 0;
+    st = cuda_status(
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_kernel, kLsmBlock, smem),
+        "occupancy(lsm)");
+    if (st) return st;
+    if ((long long)occ * c->sm_count < G)
+      return set_error(PCF_EINVAL, "LSM grid of %d blocks cannot be co-resident", G);
+    hybrid_shape(Lm, N / 2, M, G, smem, hcl, Gh, PBh);
+  }
   const int Gmax = std::max(G, Gh);
 
   LsmParams P;
   lsm_fill(P, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, 0);
   P.pairs_per_block = PB;
   P.nblocks = G;
-  // Resident path matrix: M rows x 2*Hp floats.
-  const size_t paths_bytes = sizeof(float) * (size_t)M * 2 * (size_t)P.Hp;
+  // Resident path matrix: M rows x 2*Hp floats (the streaming sweep adds
+  // 2*Hp cash flows and 2*Hp exercise dates).
+  const size_t matrix_bytes = a256(sizeof(float) * (size_t)M * 2 * (size_t)P.Hp);
+  const size_t paths_bytes =
+      matrix_bytes + (streaming ? a256(8 * (size_t)P.Hp) + a256(4 * (size_t)P.Hp) : 0);
   if (paths_bytes > c->paths_cap) {
     if (c->d_paths) cudaFree(c->d_paths);
     c->d_paths = nullptr;
@@ -1318,8 +1529,17 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   P.err = (int*)(cnt + 2);
   P.singular = (int*)(cnt + 3);
   P.out = (double*)(d + o_out);
-  bool used = false;
-  st = launch_coop(P, G, PB, smem, hcl, Gh, PBh, c->stream, &used);
+  if (streaming) {
+    P.gcf = (float*)((char*)c->d_paths + matrix_bytes);
+    P.gtau = (unsigned short*)((char*)c->d_paths + matrix_bytes + a256(8 * (size_t)P.Hp));
+    void* args[] = {&P};
+    st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_stream_kernel, dim3(G),
+                                                 dim3(kLsmBlock), args, smem, c->stream),
+                     "lsm streaming launch");
+  } else {
+    bool used = false;
+    st = launch_coop(P, G, PB, smem, hcl, Gh, PBh, c->stream, &used);
+  }
   if (st) return st;
   c->launches += 1;
   st = cuda_status(cudaMemcpyAsync(h + o_cnt, d + o_cnt, o_out - o_cnt + sizeof(double) * kMoments,

@@ -104,17 +104,17 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
 // g = payoff of the geometric mean exp(sum_m w_m log S_m): mode 0 uses the
 // trapezoid weights (w_M = 1/(2M), S_0's weight multiplies log S0/S0 = 0),
 // mode 1 equal weights 1/M on S_1..S_M.
-// One monitoring step of an Asian path (see asia_item).
+// One monitoring step of an Asian path (see asia_item). I accumulates the
+// running sum in units of S0 (S/S0 = 2^L); the path multiplies by S0 once.
 template <int MODE, bool CV>
 __device__ __forceinline__ void asia_step(const McContract& C, float w, float z, float& L,
                                           float& I, float& lg) {
   if (MODE == 0) {
-    const float S = C.S0 * ex2_approx(L);
-    I = fmaf(S, fmaf(C.c2, z, C.c1), I);
+    I = fmaf(ex2_approx(L), fmaf(C.c2, z, C.c1), I);
     L += fmaf(C.b2, z, C.a2);
   } else {
     L += fmaf(C.b2, z, C.a2);
-    I += C.S0 * ex2_approx(L);
+    I += ex2_approx(L);
   }
   if (CV) lg = fmaf(w, L, lg);
 }
@@ -141,7 +141,7 @@ __device__ __forceinline__ void asia_path(const McContract& C, const RngKey& key
   }
   // Mode 0's trapezoid weight on the last level is w_last, not w.
   if (CV && MODE == 0) lg = fmaf(C.w_last - w, L, lg);
-  const float Y = payoff(C, I * w);
+  const float Y = payoff(C, I * (C.S0 * w));
   const float G = CV ? payoff(C, C.S0 * ex2_approx(lg)) : 0.f;
   mo.add(Y, G);
 }

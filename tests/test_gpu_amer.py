@@ -42,6 +42,29 @@ def test_amer_matches_fp64_twin(orc, ctx, pf, N, M):
         assert abs(res.sums[k] - s[k]) <= tol * abs(s[k]), (k, res.sums[k], s[k])
 
 
+def test_amer_streaming_sweep_matches_fp64_twin(orc, ctx):
+    """3.2e6 paths (a point of the reference's runscript_mc_amer.sh grid): the
+    per-block slice exceeds shared memory, so the sweep streams its per-path
+    state through device memory; the same bar as the shared-memory kernels."""
+    from parcompfin_gb300 import mc_amer_result
+    N, M = 3_200_000, 10
+    res = mc_amer_result(100, 100, .05, .3, 1.0, N, M, -1, seed=5, ctx=ctx)
+    s = twin(orc, 100, 100, .05, .3, 1.0, N, M, -1, 0, 5)
+    assert s[5] == 0
+    for k in (0, 2):
+        assert abs(res.sums[k] - s[k]) <= 3e-4 * abs(s[k]), (k, res.sums[k], s[k])
+
+
+def test_amer_streaming_sweep_against_lattice(orc, ctx):
+    from parcompfin_gb300 import mc_amer_result
+    lat = orc.ref_binom_vanilla_amer(100, 100, .05, .3, 1.0, 2000, -1.0)
+    res = mc_amer_result(100, 100, .05, .3, 1.0, 4_000_000, 200, "put", seed=3, use_cv=True,
+                         ctx=ctx)
+    assert res.n_paths == 4_000_000
+    assert abs(res.price_plain - lat) < 0.05 + 4 * res.std_error_plain, (res.price_plain, lat)
+    assert abs(res.price_cv - lat) < 0.05 + 4 * res.std_error_cv, (res.price_cv, lat)
+
+
 def test_amer_put_against_lattice(orc, ctx):
     from parcompfin_gb300 import mc_amer_result
     lat = orc.ref_binom_vanilla_amer(100, 100, .05, .3, 1.0, 2000, -1.0)
