@@ -1062,6 +1062,26 @@ bool coop_shape(const pcf_ctx* c, const LsmLimits& Lm, long long H, int M, int& 
   return lsm_fits(Lm, PB, M, 2, Lm.stat_coop, 1);
 }
 
+// Grid of the streaming sweep (lsm_stream_kernel) for a contract of H pairs:
+// one block per SM (cooperative), the pairs split evenly in multiples of 4.
+int stream_shape(const pcf_ctx* c, long long H, int M, int& G, int& PB, size_t& smem) {
+  smem = sizeof(float) * 2 * (size_t)(M + 1);
+  int occ = 0;
+  const int st = cuda_status(
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_stream_kernel, kLsmBlock, smem),
+      "occupancy(lsm stream)");
+  if (st) return st;
+  if (occ < 1) return set_error(PCF_EINVAL, "the streaming LSM block does not fit on an SM");
+  const long long G0 = std::min((long long)c->sm_count, (H + 3) / 4);
+  PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
+  G = (int)((H + PB - 1) / PB);
+  return PCF_OK;
+}
+
+// Bytes after a contract's path matrix that the streaming sweep keeps its
+// per-path state in: 2*Hp cash flows, then 2*Hp exercise dates.
+size_t stream_state_bytes(long long Hp) { return a256(8 * (size_t)Hp) + a256(4 * (size_t)Hp); }
+
 // A grid of whole clusters for the two-level exchange
 // (lsm_coop_cluster_kernel) of one contract of H pairs whose plain
 // cooperative grid is G blocks of `smem` bytes: as many clusters of 8 (else 4)
@@ -1202,6 +1222,7 @@ struct LsmBatch {
   std::vector<LsmCluster> clusters;
   std::vector<LsmParams> coop;  // contracts too large for one cluster
   std::vector<int> coop_grid, coop_pb, coop_hcl, coop_gh, coop_pbh;
+  std::vector<char> coop_stream;  // runs the streaming sweep
   std::vector<size_t> coop_smem;
   void* d_mem = nullptr;
   size_t bytes = 0;
@@ -1213,6 +1234,7 @@ struct LsmLayout {
   std::vector<int> group;  // launch group of each contract, -1: cooperative kernel
   std::vector<std::vector<int>> members;
   std::vector<size_t> o_params, o_dt, o_paths, o_coop;
+  std::vector<char> stream;  // cooperative contract that runs the streaming sweep
   std::vector<int> coop_G, coop_PB, coop_hcl, coop_Gh, coop_PBh;
   std::vector<size_t> coop_sm;
   size_t upload = 0, total = 0;
@@ -1259,12 +1281,18 @@ int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
   L.coop_PBh.assign(n, 0);
   L.coop_sm.assign(n, 0);
   L.o_coop.assign(n, 0);
+  L.stream.assign(n, 0);
   for (size_t i = 0; i < n; ++i) {
     if (L.group[i] >= 0) continue;
-    if (!coop_shape(c, Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i], L.coop_sm[i]))
-      return set_error(PCF_EINVAL, "American request with N = %lld is too large", reqs[i].N);
-    hybrid_shape(Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_sm[i], L.coop_hcl[i],
-                 L.coop_Gh[i], L.coop_PBh[i]);
+    if (coop_shape(c, Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i], L.coop_sm[i])) {
+      hybrid_shape(Lm, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_sm[i], L.coop_hcl[i],
+                   L.coop_Gh[i], L.coop_PBh[i]);
+    } else {
+      const int st = stream_shape(c, reqs[i].N / 2, reqs[i].M, L.coop_G[i], L.coop_PB[i],
+                                  L.coop_sm[i]);
+      if (st) return st;
+      L.stream[i] = 1;
+    }
     const size_t gm = (size_t)std::max(L.coop_G[i], L.coop_Gh[i]);
     L.o_coop[i] = off;  // partial (2 G 8 float2) | fpartial (G 5 float2) | 2 counters
     off = a256(off + 8 * (2 * gm * kRegSums + gm * kMoments) + 16);
@@ -1274,6 +1302,7 @@ int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
     L.o_paths[i] = off;
     const long long Hp = ((reqs[i].N / 2) + 3) & ~3LL;
     off = a256(off + sizeof(float) * (size_t)reqs[i].M * 2 * (size_t)Hp);
+    if (L.stream[i]) off += stream_state_bytes(Hp);
   }
   L.total = std::max(off, (size_t)256);
   return PCF_OK;
@@ -1366,6 +1395,12 @@ int lsm_batch_create(pcf_ctx* c, const std::vector<LsmRequest>& reqs, cudaStream
     unsigned* cnt = (unsigned*)(base + 8 * (2 * gm * kRegSums + gm * kMoments));
     P.barrier = cnt;
     P.ticket = cnt + 1;
+    if (Lo.stream[i]) {
+      const size_t mb = a256(sizeof(float) * (size_t)P.M * 2 * (size_t)P.Hp);
+      P.gcf = (float*)(d + Lo.o_paths[i] + mb);
+      P.gtau = (unsigned short*)(d + Lo.o_paths[i] + mb + a256(8 * (size_t)P.Hp));
+    }
+    B->coop_stream.push_back(Lo.stream[i]);
     B->coop.push_back(P);
     B->coop_grid.push_back(Lo.coop_G[i]);
     B->coop_pb.push_back(Lo.coop_PB[i]);
@@ -1420,9 +1455,19 @@ int lsm_batch_launch_coop(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
     LsmParams& P = B->coop[i];
     st = cuda_status(cudaMemsetAsync(P.barrier, 0, 2 * sizeof(unsigned), s), "memset LSM counters");
     if (st) return st;
-    bool used = false;
-    st = launch_coop(P, B->coop_grid[i], B->coop_pb[i], B->coop_smem[i], B->coop_hcl[i],
-                     B->coop_gh[i], B->coop_pbh[i], s, &used);
+    if (B->coop_stream[i]) {
+      P.pairs_per_block = B->coop_pb[i];
+      P.nblocks = B->coop_grid[i];
+      void* args[] = {&P};
+      st = cuda_status(cudaLaunchCooperativeKernel((void*)lsm_stream_kernel,
+                                                   dim3(B->coop_grid[i]), dim3(kLsmBlock), args,
+                                                   B->coop_smem[i], s),
+                       "lsm streaming launch");
+    } else {
+      bool used = false;
+      st = launch_coop(P, B->coop_grid[i], B->coop_pb[i], B->coop_smem[i], B->coop_hcl[i],
+                       B->coop_gh[i], B->coop_pbh[i], s, &used);
+    }
     if (st) return st;
     c->launches += 1;
   }
@@ -1459,17 +1504,8 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   const bool streaming = !coop_shape(c, Lm, N / 2, M, G, PB, smem);
   int hcl = 0, Gh = 0, PBh = 0;
   if (streaming) {
-    smem = sizeof(float) * 2 * (size_t)(M + 1);
-    int occ = 0;
-    st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lsm_stream_kernel,
-                                                                   kLsmBlock, smem),
-                     "occupancy(lsm stream)");
+    st = stream_shape(c, N / 2, M, G, PB, smem);
     if (st) return st;
-    if (occ < 1) return set_error(PCF_EINVAL, "the streaming LSM block does not fit on an SM");
-    const long long H = N / 2;
-    const long long G0 = std::min((long long)c->sm_count, (H + 3) / 4);
-    PB = (int)((((H + G0 - 1) / G0) + 3) & ~3LL);
-    G = (int)((H + PB - 1) / PB);
   } else {
     int occ = 0;
     st = cuda_status(
@@ -1489,8 +1525,7 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   // Resident path matrix: M rows x 2*Hp floats (the streaming sweep adds
   // 2*Hp cash flows and 2*Hp exercise dates).
   const size_t matrix_bytes = a256(sizeof(float) * (size_t)M * 2 * (size_t)P.Hp);
-  const size_t paths_bytes =
-      matrix_bytes + (streaming ? a256(8 * (size_t)P.Hp) + a256(4 * (size_t)P.Hp) : 0);
+  const size_t paths_bytes = matrix_bytes + (streaming ? stream_state_bytes(P.Hp) : 0);
   if (paths_bytes > c->paths_cap) {
     if (c->d_paths) cudaFree(c->d_paths);
     c->d_paths = nullptr;

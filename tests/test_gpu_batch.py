@@ -146,3 +146,23 @@ def test_plan_graph_with_a_cooperative_contract(orc, ctx):
     s = (C.c_double * 6)()
     orc.twin_mc_amer(100, 100, .05, .3, 1.0, 1 << 19, 50, -1, 0, 5, 0, s)
     assert abs(again[0].sums[0] - s[0]) <= 3e-4 * abs(s[0])
+
+
+def test_batch_with_a_streaming_contract(ctx):
+    """An American contract beyond shared memory (3.2e6 paths) in a batch runs
+    the streaming sweep on the same grid as pricing it alone: the same sums."""
+    import parcompfin_gb300 as pcf
+    from parcompfin_gb300 import mc_amer_result
+    N, M = 3_200_000, 10
+    reqs = [pcf.request("eur", 100, 95, .05, .2, 1.0, 100_000, "call", seed=1, stream=1),
+            pcf.request("amer", 100, 100, .05, .3, 1.0, N, "put", M=M, seed=5, stream=0),
+            pcf.request("amer", 100, 105, .05, .3, 1.0, 1 << 16, "put", M=M, seed=5, stream=2)]
+    with pcf.Plan(reqs, ctx=ctx) as plan:
+        plan.launch()
+        got = plan.results()
+        plan.launch()
+        again = plan.results()
+    alone = mc_amer_result(100, 100, .05, .3, 1.0, N, M, -1, seed=5, ctx=ctx)
+    assert list(got[1].sums) == list(alone.sums)
+    for x, y in zip(got, again):
+        assert list(x.sums) == list(y.sums)
