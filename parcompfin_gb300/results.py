@@ -259,8 +259,13 @@ def main(argv=None) -> int:
     ap.add_argument("--svg-prefix", help="write <prefix>_time.svg and <prefix>_error.svg")
     ap.add_argument("--parallel", type=int, default=None,
                     help="plot only this thread / process count")
+    ap.add_argument("--method", action="append", default=None,
+                    help="keep only runs with this Method label (repeatable)")
     a = ap.parse_args(argv)
     ref, gpu = load(a.ref), load(a.gpu)
+    if a.method:
+        ref = [r for r in ref if r["Method"] in a.method]
+        gpu = [r for r in gpu if r["Method"] in a.method]
     rows = compare(ref, gpu)
     only_ref, only_gpu = unmatched(ref, gpu)
     if a.md:

@@ -114,3 +114,10 @@ def test_command_line(files, tmp_path, capsys):
     assert md.read_text().startswith("| Method |")
     assert (tmp_path / "s_time.svg").exists() and (tmp_path / "s_error.svg").exists()
     assert "3 parameter sets in both" in capsys.readouterr().out
+
+
+def test_command_line_method_filter(files, tmp_path, capsys):
+    md = tmp_path / "t.md"
+    assert results.main([files[0], files[1], "--md", str(md), "--method", "OMP"]) == 0
+    body = md.read_text().strip().splitlines()[2:]
+    assert len(body) == 1 and body[0].startswith("| OMP |")
