@@ -357,7 +357,12 @@ size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int ensure_tables(pcf_ctx* c, int nmax) {
   if (c->d_logtab && c->logtab_n >= nmax) return PCF_OK;
-  const int want = std::max(nmax, std::min(kMaxN, 200000));
+  // Grown by doubling from 4096 entries: a one-off small N builds a small
+  // table (its build is ~0.1 microsecond per entry and binade), a sequence
+  // of growing N rebuilds it a logarithmic number of times.
+  int want = 4096;
+  while (want < nmax && want < kMaxN) want *= 2;
+  want = std::min(std::max(want, nmax), kMaxN);
   HostTables H;
   build_tables(want, H);
   const size_t b_log = sizeof(double) * (want + 1);
