@@ -94,7 +94,8 @@ struct LsmParams {
   double* fpartial;       // nblocks x kMoments (cooperative)
   unsigned* barrier;
   unsigned* ticket;
-  int* err;               // 1: a barrier wait gave up, 2: a bulk copy wait gave up
+  int* err;               // 1: a barrier wait gave up, 2: a bulk copy wait gave up,
+                          // 4: the launch lacked its cluster shape (nothing computed)
   int* singular;          // dates whose normal equations had det <= 0
   double* out;            // kMoments sums
   float* gcf;             // streaming sweep: 2*Hp discounted cash flows (device memory)
@@ -415,6 +416,65 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
   }
 }
 
+// Antithetic pair p over the contract's M dates (path p takes +z, path p + H
+// takes -z, as pathsfinder pairs them): writes the signed moneyness
+// u = pf (S/E - 1) of both paths to the path matrix, one row per date, and
+// returns u at date M of the plus and the minus path. Date m0 + l + 1 takes
+// lane l of Philox block m0 / 4: whole blocks first, without per-date checks,
+// then the last 1..3 dates.
+__device__ __forceinline__ float2 forward_pair(const LsmParams& P, const RngKey& key,
+                                               long long p) {
+  const size_t stride = (size_t)2 * P.Hp;  // floats per row
+  const float nb2 = -P.b2;
+  const int M = P.M;
+  float Lp = 0.f, Lm = 0.f, Up = 0.f, Um = 0.f;
+  float* row = P.paths + p;
+  auto step = [&](float z) {
+    Lp += fmaf(P.b2, z, P.a2);
+    Lm += fmaf(nb2, z, P.a2);
+    Up = fmaf(P.pf, ex2_approx(P.l2SE + Lp), -P.pf);  // pf (S/E - 1)
+    Um = fmaf(P.pf, ex2_approx(P.l2SE + Lm), -P.pf);
+    row[0] = Up;
+    row[P.Hp] = Um;
+    row += stride;
+  };
+  const int Mfull = M & ~3;
+  for (int m0 = 0; m0 < Mfull; m0 += 4) {
+    const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(m0 >> 2)));
+    step(z4.x);
+    step(z4.y);
+    step(z4.z);
+    step(z4.w);
+  }
+  if (Mfull < M) {
+    const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(Mfull >> 2)));
+    step(z4.x);
+    if (Mfull + 1 < M) step(z4.y);
+    if (Mfull + 2 < M) step(z4.z);
+  }
+  return make_float2(Up, Um);
+}
+
+// The control-variate sample of one path with exercise date tau, cash flow
+// cfd (discounted to 0) and moneyness uM at date M. Martingale control
+// variate: g = e^{-r tau} P_E(S_tau, T - tau), the discounted European price
+// at the path's exercise time; the discounted European price is a martingale,
+// so E[g] = P_E(S0, T) for any stopping time. S_tau is E + pf*cf where the
+// path exercised before T; a path held to T (tau = M) contributes its
+// discounted payoff at T, which is cfd.
+__device__ __forceinline__ float cv_sample(const LsmParams& P, const float* dt, const float* edt,
+                                           int tau, float cfd, float uM) {
+  const int M = P.M;
+  if (P.ref_exercise) {
+    // The reference's exercise value does not identify S_tau: use the
+    // discounted European payoff at T (mean: the same P_E(S0, T)).
+    return dt[M] * (P.E * fmaxf(uM, 0.f));
+  }
+  if (tau == M) return cfd;  // the discounted European payoff at T
+  const float St = P.E + P.pf * (cfd * edt[tau]);
+  return dt[tau] * european_price(P, St, (float)(M - tau) * P.dtf);
+}
+
 // One contract's forward pass, backward sweep and final moments, executed by
 // block `b` of the contract's `P.nblocks` blocks. Every wait is bounded. A
 // cooperative block that gave up leaves after its in-flight copies landed; a
@@ -454,39 +514,11 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
   const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
   const float EdM = P.E * P.dtab[M];  // payoff at T = E max(u, 0), discounted
   const size_t stride = (size_t)2 * P.Hp;  // floats per row
-  const float nb2 = -P.b2;
 #pragma unroll 2
   for (int i = threadIdx.x; i < nb; i += BS) {
-    const long long p = p0 + i;
-    float Lp = 0.f, Lm = 0.f, Up = 0.f, Um = 0.f;
-    float* row = P.paths + p;
-    // Date m0 + l + 1 takes lane l of Philox block m0 / 4: whole blocks first,
-    // without per-date checks, then the last 1..3 dates.
-    auto step = [&](float z) {
-      Lp += fmaf(P.b2, z, P.a2);
-      Lm += fmaf(nb2, z, P.a2);
-      Up = fmaf(P.pf, ex2_approx(P.l2SE + Lp), -P.pf);  // pf (S/E - 1)
-      Um = fmaf(P.pf, ex2_approx(P.l2SE + Lm), -P.pf);
-      row[0] = Up;
-      row[P.Hp] = Um;
-      row += stride;
-    };
-    const int Mfull = M & ~3;
-    for (int m0 = 0; m0 < Mfull; m0 += 4) {
-      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(m0 >> 2)));
-      step(z4.x);
-      step(z4.y);
-      step(z4.z);
-      step(z4.w);
-    }
-    if (Mfull < M) {
-      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(Mfull >> 2)));
-      step(z4.x);
-      if (Mfull + 1 < M) step(z4.y);
-      if (Mfull + 2 < M) step(z4.z);
-    }
-    S.cf[i] = fmaxf(Up, 0.f) * EdM;
-    S.cf[PB + i] = fmaxf(Um, 0.f) * EdM;
+    const float2 uM = forward_pair(P, key, p0 + i);
+    S.cf[i] = fmaxf(uM.x, 0.f) * EdM;
+    S.cf[PB + i] = fmaxf(uM.y, 0.f) * EdM;
     S.tau[i] = (TauT)M;
     S.tau[PB + i] = (TauT)M;
   }
@@ -636,11 +668,6 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
   // ---- discounted cash flows and the control variate, per antithetic pair ----
   // Moments are taken over pair means: the two paths of a pair share their
   // draws, so the pair, not the path, is the independent sample.
-  // Control variate (martingale CV): g = e^{-r tau} P_E(S_tau, T - tau), the
-  // discounted European price at the path's exercise time. The discounted
-  // European price is a martingale, so E[g] = P_E(S0, T) for any stopping
-  // time. S_tau is E + pf*cf where the path exercised (or finished in the
-  // money) and S_M from the last row otherwise.
   const float* last = P.paths + (size_t)(M - 1) * 2 * P.Hp;
   KSum sy, syy, sg, sgg, syg;
   for (int i = threadIdx.x; i < nb; i += BS) {
@@ -648,21 +675,10 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int s = h * PB + i;
-      const int tau = S.tau[s];
       const float cfd = S.cf[s];  // cash flow discounted to time 0
       y2 += cfd;
-      float g;
-      if (P.ref_exercise) {
-        // The reference's exercise value does not identify S_tau: use the
-        // discounted European payoff at T (mean: the same P_E(S0, T)).
-        g = S.dt[M] * (P.E * fmaxf(last[h * P.Hp + p0 + i], 0.f));
-      } else if (tau == M) {
-        g = cfd;  // the discounted European payoff at T
-      } else {
-        const float St = P.E + P.pf * (cfd * S.edt[tau]);
-        g = S.dt[tau] * european_price(P, St, (float)(M - tau) * P.dtf);
-      }
-      g2 += g;
+      g2 += cv_sample(P, S.dt, S.edt, S.tau[s], cfd,
+                      P.ref_exercise ? last[h * P.Hp + p0 + i] : 0.f);
     }
     const float y = 0.5f * y2, g = 0.5f * g2;
     sy.add(y);
@@ -702,6 +718,12 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_kernel(LsmParams P) {
 // per date the CTAs of a cluster exchange through distributed shared memory,
 // and only the clusters' leaders meet in global memory.
 __global__ void __launch_bounds__(kLsmBlock, 1) lsm_coop_cluster_kernel(LsmParams P) {
+  // The exchange addresses P.cluster peers: a launch without that cluster
+  // shape stops here with an error instead of addressing absent CTAs.
+  if (cg::this_cluster().num_blocks() != (unsigned)P.cluster) {
+    if (threadIdx.x == 0) atomicExch(P.err, 4);
+    return;
+  }
   lsm_body<kCoopCluster, unsigned short, kLsmBlock>(P, blockIdx.x,
                                                     (int)cg::this_cluster().block_rank());
 }
@@ -736,36 +758,11 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
   const RngKey key{P.seed_lo, P.seed_hi, P.stream, TAG_AMER};
   const float EdM = P.E * P.dtab[M];
   const size_t stride = (size_t)2 * Hp;
-  const float nb2 = -P.b2;
   for (long long i = threadIdx.x; i < nb; i += BS) {
     const long long p = p0 + i;
-    float Lp = 0.f, Lm = 0.f, Up = 0.f, Um = 0.f;
-    float* row = P.paths + p;
-    auto step = [&](float z) {
-      Lp += fmaf(P.b2, z, P.a2);
-      Lm += fmaf(nb2, z, P.a2);
-      Up = fmaf(P.pf, ex2_approx(P.l2SE + Lp), -P.pf);
-      Um = fmaf(P.pf, ex2_approx(P.l2SE + Lm), -P.pf);
-      row[0] = Up;
-      row[Hp] = Um;
-      row += stride;
-    };
-    const int Mfull = M & ~3;
-    for (int m0 = 0; m0 < Mfull; m0 += 4) {
-      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(m0 >> 2)));
-      step(z4.x);
-      step(z4.y);
-      step(z4.z);
-      step(z4.w);
-    }
-    if (Mfull < M) {
-      const float4 z4 = normals4(draw_words(key, (uint64_t)p, (uint32_t)(Mfull >> 2)));
-      step(z4.x);
-      if (Mfull + 1 < M) step(z4.y);
-      if (Mfull + 2 < M) step(z4.z);
-    }
-    P.gcf[p] = fmaxf(Up, 0.f) * EdM;
-    P.gcf[Hp + p] = fmaxf(Um, 0.f) * EdM;
+    const float2 uM = forward_pair(P, key, p);
+    P.gcf[p] = fmaxf(uM.x, 0.f) * EdM;
+    P.gcf[Hp + p] = fmaxf(uM.y, 0.f) * EdM;
     P.gtau[p] = (unsigned short)M;
     P.gtau[Hp + p] = (unsigned short)M;
   }
@@ -870,19 +867,9 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const long long s = h * Hp + p0 + i;
-      const int tau = P.gtau[s];
       const float cfd = P.gcf[s];
       y2 += cfd;
-      float g;
-      if (P.ref_exercise) {
-        g = dt[M] * (P.E * fmaxf(last[s], 0.f));
-      } else if (tau == M) {
-        g = cfd;
-      } else {
-        const float St = P.E + P.pf * (cfd * edt[tau]);
-        g = dt[tau] * european_price(P, St, (float)(M - tau) * P.dtf);
-      }
-      g2 += g;
+      g2 += cv_sample(P, dt, edt, P.gtau[s], cfd, P.ref_exercise ? last[s] : 0.f);
     }
     const float y = 0.5f * y2, g = 0.5f * g2;
     sy.add(y);
@@ -902,10 +889,18 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
 // one runs its per-date exchange and solve, the other's paths keep the SM
 // busy.
 template <typename TauT>
-__global__ void __launch_bounds__(kLsmCBlock, 2) lsm_cluster_kernel(const LsmParams* __restrict__ cs) {
+__global__ void __launch_bounds__(kLsmCBlock, 2)
+    lsm_cluster_kernel(const LsmParams* __restrict__ cs, int C) {
   __shared__ LsmParams sP;  // the contract's parameters, read from shared memory
   const unsigned rank = cg::this_cluster().block_rank();
-  const int c = (int)(blockIdx.x / cg::this_cluster().num_blocks());
+  const unsigned CL = cg::this_cluster().num_blocks();
+  // Every contract of the launch has cs[0].nblocks CTAs, one cluster each; a
+  // launch of another shape stops with an error instead of mixing contracts.
+  if (CL != (unsigned)cs[0].nblocks || gridDim.x != (unsigned)C * CL) {
+    if (threadIdx.x == 0 && blockIdx.x < (unsigned)C) atomicExch(cs[blockIdx.x].err, 4);
+    return;
+  }
+  const int c = (int)(blockIdx.x / CL);
   if (threadIdx.x == 0) sP = cs[c];
   __syncthreads();
   lsm_body<kCluster, TauT, kLsmCBlock>(sP, (int)rank, (int)rank);
@@ -1440,8 +1435,9 @@ int lsm_batch_launch_clusters(pcf_ctx* c, LsmBatch* B, cudaStream_t s) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     const LsmParams* prm = L.d_params;
-    st = cuda_status(L.t8 ? cudaLaunchKernelEx(&cfg, lsm_cluster_kernel<unsigned char>, prm)
-                          : cudaLaunchKernelEx(&cfg, lsm_cluster_kernel<unsigned short>, prm),
+    const int C = L.C;
+    st = cuda_status(L.t8 ? cudaLaunchKernelEx(&cfg, lsm_cluster_kernel<unsigned char>, prm, C)
+                          : cudaLaunchKernelEx(&cfg, lsm_cluster_kernel<unsigned short>, prm, C),
                      "lsm cluster launch");
     if (st) return st;
     c->launches += 1;
@@ -1583,6 +1579,7 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "lsm kernel");
   if (st) return st;
   const int* flags = (const int*)(h + o_cnt);
+  if (flags[2] == 4) return set_error(PCF_ECUDA, "LSM cluster launch ran without its cluster shape");
   if (flags[2]) return set_error(PCF_ETIMEOUT, "LSM device wait gave up (code %d)", flags[2]);
   if (flags[3])
     return set_error(PCF_ESINGULAR, "Detereminant is not > 0 at %d exercise date(s)", flags[3]);

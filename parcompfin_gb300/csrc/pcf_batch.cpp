@@ -404,8 +404,10 @@ int plan_fill_results(pcf_plan* p, pcf_mc_result* results) {
       // A request whose sweep failed gets NaN; the call reports the first failure.
       results[i].price = results[i].price_plain = results[i].price_cv = NAN;
       if (status == PCF_OK)
-        status = set_error(fl[0] ? PCF_ETIMEOUT : PCF_ESINGULAR, "request %d: %s", i,
-                           fl[0] ? "LSM device wait gave up" : "Detereminant is not > 0");
+        status = fl[0] == 4 ? set_error(PCF_ECUDA, "request %d: LSM cluster launch ran without "
+                                        "its cluster shape", i)
+                 : set_error(fl[0] ? PCF_ETIMEOUT : PCF_ESINGULAR, "request %d: %s", i,
+                             fl[0] ? "LSM device wait gave up" : "Detereminant is not > 0");
     }
   }
   return status;
