@@ -55,6 +55,17 @@ def test_amer_streaming_sweep_matches_fp64_twin(orc, ctx):
         assert abs(res.sums[k] - s[k]) <= 3e-4 * abs(s[k]), (k, res.sums[k], s[k])
 
 
+def test_amer_streaming_sweep_reference_rule_call_matches_fp64_twin(orc, ctx):
+    """The streaming sweep with the reference's exercise rule, on a call."""
+    from parcompfin_gb300 import mc_amer_result
+    N, M = 3_200_000, 8
+    res = mc_amer_result(100, 95, .05, .3, 1.0, N, M, 1, ref_exercise=True, seed=6, ctx=ctx)
+    s = twin(orc, 100, 95, .05, .3, 1.0, N, M, 1, 1, 6)
+    assert s[5] == 0
+    for k in (0, 2):
+        assert abs(res.sums[k] - s[k]) <= 1e-3 * abs(s[k]), (k, res.sums[k], s[k])
+
+
 def test_amer_streaming_sweep_against_lattice(orc, ctx):
     from parcompfin_gb300 import mc_amer_result
     lat = orc.ref_binom_vanilla_amer(100, 100, .05, .3, 1.0, 2000, -1.0)

@@ -99,3 +99,39 @@ def test_serving_without_target_uses_request_sizes(ctx):
     assert st.completed == 20
     for q, o in zip(reqs, out):
         assert o.result.n_paths == q["N"] and o.paths == q["N"]
+
+
+def test_request_whose_pilot_reaches_the_target_is_done_after_it(ctx):
+    """A deep in-the-money European call with its control variate (g = S_T)
+    has almost no residual variance: the pilot's 2^14 paths already reach the
+    target, so the pilot is its result."""
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("eur", 100, 20, .05, .2, 1.0, 4, "call", use_cv=True, seed=3, stream=0),
+            pcf.request("eur", 100, 100, .05, .2, 1.0, 4, "call", use_cv=True, seed=3, stream=1)]
+    out, st = pcf.serve_trace(reqs, [0.0, 0.0], target_rel_se=TARGET, ctx=ctx)
+    assert st.completed == 2
+    deep, atm = out[0], out[1]
+    assert deep.result.n_paths == PILOT and deep.paths == PILOT
+    assert deep.result.std_error / deep.result.price < TARGET
+    alone = pcf.price_batch([dict(reqs[0], N=PILOT)], ctx=ctx)[0]
+    assert list(alone.sums) == list(deep.result.sums)
+    assert atm.result.n_paths > PILOT and atm.paths == atm.result.n_paths
+
+
+def test_price_batch_arena_grows_and_is_reused(ctx):
+    """pcf_price_batch builds in the context's arena: a small batch, a much
+    larger one (the arena grows), then the small one again give the same sums
+    as plans built on their own."""
+    import parcompfin_gb300 as pcf
+    small = [pcf.request("eur", 100, 100, .05, .2, 1.0, 100_000, "call", seed=1, stream=0)]
+    big = [pcf.request("amer", 100, 95 + k, .05, .3, 1.0, 1 << 18, "put", M=50, seed=2, stream=k)
+           for k in range(12)] + small
+    a = pcf.price_batch(small, ctx=ctx)
+    b = pcf.price_batch(big, ctx=ctx)
+    c = pcf.price_batch(small, ctx=ctx)
+    with pcf.Plan(big, ctx=ctx) as plan:
+        plan.launch()
+        ref = plan.results()
+    assert list(a[0].sums) == list(c[0].sums) == list(b[-1].sums)
+    for x, y in zip(b, ref):
+        assert list(x.sums) == list(y.sums)
