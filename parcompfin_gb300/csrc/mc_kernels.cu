@@ -222,22 +222,18 @@ __device__ __forceinline__ void basket_path(const McContract& C, const float* fb
 }
 
 // Basket item j covers paths [j*U, (j+1)*U), U = units_per_item: U/256 paths
-// per thread (path j*U + k*256 + thread) for baskets of up to 8 assets, one
-// path per thread for larger ones (their path loop would hold the whole
-// unrolled factor product in registers).
+// per thread (path j*U + k*256 + thread), one after the other (the loop is
+// not unrolled, so a path's unrolled factor product keeps its registers).
 template <int DMAX, bool CV>
 __device__ __forceinline__ void basket_item(const McContract& C, int j, const float* fb,
                                             Moments<CV>& mo) {
   const long long n0 = (long long)j * C.units_per_item + threadIdx.x;
-  if (DMAX <= 8) {
-    const int ppt = C.units_per_item / kBlock;
-    for (int k = 0; k < ppt; ++k) {
-      const long long n = n0 + (long long)k * kBlock;
-      if (n >= C.N) break;
-      basket_path<DMAX, CV>(C, fb, n, mo);
-    }
-  } else if (n0 < C.N) {
-    basket_path<DMAX, CV>(C, fb, n0, mo);
+  const int ppt = C.units_per_item / kBlock;
+#pragma unroll 1
+  for (int k = 0; k < ppt; ++k) {
+    const long long n = n0 + (long long)k * kBlock;
+    if (n >= C.N) break;
+    basket_path<DMAX, CV>(C, fb, n, mo);
   }
 }
 

@@ -203,10 +203,11 @@ int eur_quads_per_thread(long long N) {
 // Asian: at least ~256 monitoring steps per thread per item.
 int asia_paths_per_thread(int M) { return std::max(1, std::min(16, (256 + M - 1) / M)); }
 
-// Basket: a few paths per thread for baskets of up to 8 assets (the kernels
-// for 9..16 assets take one path per thread); wider baskets run the
+// Basket: 16 / 8 / 8 paths per thread for up to 4 / 8 / 16 assets (an item
+// pays one block reduction; items of one path per thread spent more than
+// half of a 16-asset path's instructions on it); wider baskets run the
 // tensor-core kernel, whose items are 8 tiles of 128 paths.
-int basket_paths_per_thread(int d) { return d <= 4 ? 8 : d <= 8 ? 4 : d <= 16 ? 1 : 4; }
+int basket_paths_per_thread(int d) { return d <= 4 ? 16 : d <= 8 ? 8 : d <= 16 ? 8 : 4; }
 
 McContract make_eur(double S0, double E, double r, double sigma, double T, long long N, int pf,
                     unsigned long long seed, uint32_t stream) {
