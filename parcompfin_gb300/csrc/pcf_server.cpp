@@ -85,11 +85,12 @@ long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 // it the regression's own noise dominates the pilot's variance estimate.
 constexpr long long kAmerFloor = 1LL << 16;
 
-// Device bytes a request's main run needs (American: its path matrix).
+// Device bytes a request's main run needs (American: its path matrix, and
+// the per-path state a streaming sweep keeps beside it).
 size_t main_bytes(const pcf_mc_request& q) {
   if (q.method != PCF_METHOD_AMER) return 4096;
   const long long Hp = ((q.N / 2) + 3) & ~3LL;
-  return (size_t)4 * q.M * 2 * Hp + 4096;
+  return (size_t)4 * q.M * 2 * Hp + (size_t)12 * Hp + 4096;
 }
 
 }  // namespace
