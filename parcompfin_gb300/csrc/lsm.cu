@@ -184,14 +184,15 @@ __device__ __forceinline__ void issue_row(const LsmParams& P, int r, long long p
 
 // Adds one path's terms to the regression sums of a date if the path is in
 // the money there (src/mc_amer.cpp:57-66 regresses on in-the-money paths
-// only): u = pf (S - E)/E and the discounted cash flow y = cfd * growth.
+// only): u = pf (S - E)/E and the cash flow discounted to time 0, y = cfd.
+// The regression target is y times the date's growth factor; the factor is
+// common to every path, so regress_date applies it once to the three y sums.
 // Paths out of the money (u <= 0) add zeros, so the loop has no divergent
 // branch.
-__device__ __forceinline__ void reg_accumulate(float u, float cfd, float growth,
-                                               float (&acc)[kRegSums]) {
+__device__ __forceinline__ void reg_accumulate(float u, float cfd, float (&acc)[kRegSums]) {
   const bool itm = u > 0.f;
   const float x = itm ? u : 0.f;
-  const float y = itm ? cfd * growth : 0.f;
+  const float y = itm ? cfd : 0.f;
   const float x2 = x * x;
   acc[0] += itm ? 1.f : 0.f;
   acc[1] += x;
@@ -256,7 +257,8 @@ __device__ __forceinline__ bool group_arrive_wait(unsigned* counter, unsigned G,
 // sums in FP64 and the solve. Leaves the mode and coefficients in X.
 template <int MODE, int NW>
 __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& X, int d, int b,
-                                             int rank, uint32_t& xph, uint32_t& xcount) {
+                                             int rank, uint32_t& xph, uint32_t& xcount,
+                                             float growth) {
   const int lane = threadIdx.x & 31;
   const int q = lane & 7;
   // Block total of sum q: lane groups l>>3 = 0..3 each add four warps' sums,
@@ -353,6 +355,7 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
   }
   g = df_add(g, shfl_xor_df(g, 8));
   g = df_add(g, shfl_xor_df(g, 16));  // lanes 0..7: the contract's sum q = lane
+  if (q >= 5) g = df_mul(g, DF{growth, 0.f});  // y sums: cash flows grown to date d
   // include/common.h:98-141 solves the normal equations by the adjugate over
   // the determinant, then a mat-vec product. The normal matrix of the basis
   // {1, u, u^2} is the symmetric Hankel matrix [[a0,a1,a2],[a1,a2,a3],
@@ -427,13 +430,13 @@ __device__ __forceinline__ float2 forward_pair(const LsmParams& P, const RngKey&
   const size_t stride = (size_t)2 * P.Hp;  // floats per row
   const float nb2 = -P.b2;
   const int M = P.M;
-  float Lp = 0.f, Lm = 0.f, Up = 0.f, Um = 0.f;
+  float Lp = P.l2SE, Lm = P.l2SE, Up = 0.f, Um = 0.f;  // log2(S/E)
   float* row = P.paths + p;
   auto step = [&](float z) {
     Lp += fmaf(P.b2, z, P.a2);
     Lm += fmaf(nb2, z, P.a2);
-    Up = fmaf(P.pf, ex2_approx(P.l2SE + Lp), -P.pf);  // pf (S/E - 1)
-    Um = fmaf(P.pf, ex2_approx(P.l2SE + Lm), -P.pf);
+    Up = fmaf(P.pf, ex2_approx(Lp), -P.pf);  // pf (S/E - 1)
+    Um = fmaf(P.pf, ex2_approx(Lm), -P.pf);
     row[0] = Up;
     row[P.Hp] = Um;
     row += stride;
@@ -571,7 +574,7 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
       if (threadIdx.x == 32) issue_row(P, next_row, p0, nbr, PB, S.slice(next_k), &S.bar[next_k]);
       pend |= 1u << next_k;
     }
-    if (wid == 0) regress_date<MODE, BS / 32>(P, X, d, b, rank, xph, xcount);
+    if (wid == 0) regress_date<MODE, BS / 32>(P, X, d, b, rank, xph, xcount, S.edt[d]);
     __syncthreads();
   };
 
@@ -582,16 +585,15 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
     const float* sl = S.slice(0);
-    const float e1 = S.edt[M - 1];
     for (int j = threadIdx.x; j < nq; j += BS) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int s = h * PB + 4 * j;
         const float4 u = ld4(sl + s), c = ld4(S.cf + s);
-        reg_accumulate(u.x, c.x, e1, acc);
-        reg_accumulate(u.y, c.y, e1, acc);
-        reg_accumulate(u.z, c.z, e1, acc);
-        reg_accumulate(u.w, c.w, e1, acc);
+        reg_accumulate(u.x, c.x, acc);
+        reg_accumulate(u.y, c.y, acc);
+        reg_accumulate(u.z, c.z, acc);
+        reg_accumulate(u.w, c.w, acc);
       }
     }
     regress(acc, M - 1, -1, 0);
@@ -605,7 +607,7 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
     if (has_next) wait_copy(k ^ 1);
     const int mode = X.mode;
     const float c0 = X.coef[0], c1 = X.coef[1], c2 = X.coef[2];
-    const float dm = S.dt[m], em = S.edt[m], e1 = S.edt[m - 1];
+    const float dm = S.dt[m], em = S.edt[m];
     const float* cur = S.slice(k);
     const float* nxt = S.slice(k ^ 1);
     float acc[kRegSums];
@@ -645,10 +647,10 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
         }
         if (has_next) {
           const float4 u = ld4(nxt + s);
-          reg_accumulate(u.x, c.x, e1, acc);
-          reg_accumulate(u.y, c.y, e1, acc);
-          reg_accumulate(u.z, c.z, e1, acc);
-          reg_accumulate(u.w, c.w, e1, acc);
+          reg_accumulate(u.x, c.x, acc);
+          reg_accumulate(u.y, c.y, acc);
+          reg_accumulate(u.z, c.z, acc);
+          reg_accumulate(u.w, c.w, acc);
         }
       }
     }
@@ -781,7 +783,7 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
     const float v = warp_scatter8(acc);
     if ((lane & 3) == 0) X.wpart[wid][lane >> 2] = v;
     __syncthreads();
-    if (wid == 0) regress_date<kCoop, NW>(P, X, d, b, 0, xph, xcount);
+    if (wid == 0) regress_date<kCoop, NW>(P, X, d, b, 0, xph, xcount, edt[d]);
     __syncthreads();
   };
   {
@@ -789,17 +791,16 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
     const float* rowd = P.paths + (size_t)(M - 2) * stride + p0;  // date M-1
-    const float e1 = edt[M - 1];
     for (long long j = threadIdx.x; j < nq; j += BS) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const long long s = h * Hp + 4 * j;
         const float4 u = __ldcs(reinterpret_cast<const float4*>(rowd + s));
         const float4 c = *reinterpret_cast<const float4*>(P.gcf + p0 + s);
-        reg_accumulate(u.x, c.x, e1, acc);
-        reg_accumulate(u.y, c.y, e1, acc);
-        reg_accumulate(u.z, c.z, e1, acc);
-        reg_accumulate(u.w, c.w, e1, acc);
+        reg_accumulate(u.x, c.x, acc);
+        reg_accumulate(u.y, c.y, acc);
+        reg_accumulate(u.z, c.z, acc);
+        reg_accumulate(u.w, c.w, acc);
       }
     }
     regress(acc, M - 1);
@@ -809,7 +810,7 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
     const bool has_next = m > 1;
     const int mode = X.mode;
     const float c0 = X.coef[0], c1 = X.coef[1], c2 = X.coef[2];
-    const float dm = dt[m], em = edt[m], e1 = edt[m - 1];
+    const float dm = dt[m], em = edt[m];
     const float* cur = P.paths + (size_t)(m - 1) * stride + p0;  // date m is row m-1
     const float* nxt = has_next ? cur - stride : cur;
     float acc[kRegSums];
@@ -845,10 +846,10 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
         }
         if (has_next) {
           const float4 u = *reinterpret_cast<const float4*>(nxt + s);
-          reg_accumulate(u.x, c.x, e1, acc);
-          reg_accumulate(u.y, c.y, e1, acc);
-          reg_accumulate(u.z, c.z, e1, acc);
-          reg_accumulate(u.w, c.w, e1, acc);
+          reg_accumulate(u.x, c.x, acc);
+          reg_accumulate(u.y, c.y, acc);
+          reg_accumulate(u.z, c.z, acc);
+          reg_accumulate(u.w, c.w, acc);
         }
       }
     }
