@@ -81,6 +81,15 @@ PCF_API int pcf_ctx_destroy(pcf_ctx* ctx);
 PCF_API void* pcf_ctx_stream(pcf_ctx* ctx);
 /* Number of kernels this context has launched so far. */
 PCF_API long long pcf_ctx_launch_count(pcf_ctx* ctx);
+/* Frees the device and pinned memory the context keeps between calls (the
+ * scratch arena, the resident LSM path matrix, the binomial tables, the
+ * serving slots); the next call that needs them allocates them again. */
+PCF_API int pcf_ctx_release(pcf_ctx* ctx);
+/* Caps each device buffer the context allocates (the scratch arena, an LSM
+ * path matrix, a plan, the serving slots' reservation) at `bytes`; a call
+ * that would need more returns PCF_ENOMEM. 0 removes the cap. Buffers held
+ * already are not shrunk: call pcf_ctx_release first. */
+PCF_API int pcf_ctx_set_memory_limit(pcf_ctx* ctx, unsigned long long bytes);
 
 /* European option, single-step GBM Monte Carlo.
  * Replaces double mc_eur(S0,E,r,sigma,T,N,payoff_fun), src/mc_eur.cpp:5-27

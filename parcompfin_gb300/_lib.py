@@ -122,6 +122,8 @@ SIGNATURES = {
     "pcf_ctx_destroy": (_I, [_P]),
     "pcf_ctx_stream": (_P, [_P]),
     "pcf_ctx_launch_count": (_LL, [_P]),
+    "pcf_ctx_release": (_I, [_P]),
+    "pcf_ctx_set_memory_limit": (_I, [_P, C.c_ulonglong]),
     "pcf_mc_eur": (_I, [_P, _D, _D, _D, _D, _D, _LL, _I, _ULL, _I, C.POINTER(McResult)]),
     "pcf_mc_asia": (_I, [_P, _D, _D, _D, _D, _D, _LL, _I, _I, _I, _ULL, _I,
                          C.POINTER(McResult)]),

@@ -66,6 +66,14 @@ class Context:
     def launches(self) -> int:
         return int(_lib.load().pcf_ctx_launch_count(self._h))
 
+    def release(self) -> None:
+        """Free the device and pinned memory kept between calls."""
+        _lib.check(_lib.load().pcf_ctx_release(self._h))
+
+    def set_memory_limit(self, nbytes: int) -> None:
+        """Cap each device buffer the context allocates (0: no cap)."""
+        _lib.check(_lib.load().pcf_ctx_set_memory_limit(self._h, int(nbytes)))
+
     def close(self) -> None:
         if self._h:
             _lib.load().pcf_ctx_destroy(self._h)

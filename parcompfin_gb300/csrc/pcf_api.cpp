@@ -371,6 +371,30 @@ long long pcf_ctx_launch_count(pcf_ctx* c) {
   return c ? c->launches : -1;
 }
 
+int pcf_ctx_release(pcf_ctx* c) {
+  int st;
+  c = resolve_ctx(c, &st);
+  if (!c) return st;
+  cudaSetDevice(c->device);
+  st = cuda_status(cudaStreamSynchronize(c->stream), "context stream");
+  serve_release(c);
+  ctx_release_extras(c);
+  if (c->d_buf) cudaFree(c->d_buf);
+  if (c->h_buf) cudaFreeHost(c->h_buf);
+  c->d_buf = nullptr;
+  c->h_buf = nullptr;
+  c->d_cap = c->h_cap = 0;
+  return st;
+}
+
+int pcf_ctx_set_memory_limit(pcf_ctx* c, unsigned long long bytes) {
+  int st;
+  c = resolve_ctx(c, &st);
+  if (!c) return st;
+  c->budget_bytes = (size_t)bytes;
+  return PCF_OK;
+}
+
 int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T, long long N,
                int payoff_fun, unsigned long long seed, int use_cv, pcf_mc_result* out) {
   if (!out) return set_error(PCF_EINVAL, "out is NULL");

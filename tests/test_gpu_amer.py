@@ -156,3 +156,23 @@ def test_amer_deterministic(ctx):
     a = mc_amer(100, 100, .05, .3, 1.0, 65536, 50, -1, seed=9, ctx=ctx)
     b = mc_amer(100, 100, .05, .3, 1.0, 65536, 50, -1, seed=9, ctx=ctx)
     assert a == b
+
+
+def test_context_release_and_memory_limit(ctx):
+    """The context keeps the LSM path matrix between calls; release frees it,
+    and a memory limit below a call's need makes that call PCF_ENOMEM while
+    smaller calls go on. The same contract prices to the same sums after."""
+    from parcompfin_gb300 import mc_amer_result, mc_eur_result
+    from parcompfin_gb300._lib import PcfError, PCF_ENOMEM
+    args = (100, 100, .05, .3, 1.0, 1 << 20, 50, -1)
+    first = mc_amer_result(*args, seed=8, ctx=ctx)     # a 210 MB path matrix
+    ctx.release()
+    ctx.set_memory_limit(64 << 20)
+    with pytest.raises(PcfError) as e:
+        mc_amer_result(*args, seed=8, ctx=ctx)
+    assert e.value.status == PCF_ENOMEM
+    small = mc_eur_result(100, 100, .05, .2, 1.0, 1 << 20, "call", seed=8, ctx=ctx)
+    assert small.price > 0
+    ctx.set_memory_limit(0)
+    again = mc_amer_result(*args, seed=8, ctx=ctx)
+    assert list(again.sums) == list(first.sums)
