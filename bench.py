@@ -75,6 +75,14 @@ def _fp32_roofline(flop_per_unit, units, ms, sms, sm_mhz):
 # --------------------------------------------------------------------------
 # workloads
 # --------------------------------------------------------------------------
+# DRAM bytes per algorithmic byte of the American cluster kernel: one
+# `ncu --set full` capture of the 64-put batch (dram__bytes_read.sum +
+# dram__bytes_write.sum = 1635.3 MB for 1677.7 MB algorithmic;
+# profiles/lsm_cluster_kernel_64_puts_2p16.md). Traffic grows with the
+# path-dates, so other launches of the kernel scale by it.
+LSM_TRAFFIC_PER_ALG_BYTE = 1635.3 / 1677.7
+
+
 class EurWorkload:
     name = "eur"
     metric = "MC paths/sec (European GBM, S0=K=100, r=.05, sigma=.2, T=1 call)"
@@ -546,7 +554,9 @@ class MixedWorkload:
         ach = alg / (t * 1e-3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": None, "kernel_ms": t,
+                "traffic": alg * LSM_TRAFFIC_PER_ALG_BYTE,
+                "traffic_source": "ncu capture of the 64-put batch, scaled by path-dates",
+                "kernel_ms": t,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
                                "fallback 6.8 TB/s",
                 "share_of_step": t / ms}
@@ -693,7 +703,9 @@ class AmerBatchWorkload:
         ach = alg / (ms * 1e-3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+                "traffic": alg * LSM_TRAFFIC_PER_ALG_BYTE,
+                "traffic_source": "ncu capture of this launch (dram bytes read + written)",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
 
     def cpu_reference(self, threads, budget_s):
         return LsmWorkload.cpu_reference(self, threads, budget_s)
