@@ -504,7 +504,7 @@ class MixedWorkload:
         if not hasattr(self, "_e2e_in"):
             arr, keep = api._pack(self.base)
             self._e2e_in = (arr, keep, (C.c_double * n)(*([0.0] * n)),
-                            _lib.ServerConfig(self.TARGET, 1 << 14, 1 << 26, 1 << 21, 2048, 8, 0.5),
+                            _lib.ServerConfig(self.TARGET, 1 << 14, 1 << 26, 1 << 21, 2048, 12, 0.5),
                             (_lib.ServedResult * n)(), _lib.ServerStats())
         arr, _, arrival, cfg, out, stats = self._e2e_in
         st = _lib.load().pcf_serve_trace(api._h(ctx), C.byref(cfg), n, arr, arrival, out,

@@ -266,7 +266,7 @@ typedef struct pcf_server_config {
   long long max_paths;      /* 0: 2^26 */
   long long max_amer_paths; /* 0: 2^21 */
   int max_batch;            /* requests per batch; 0: 2048 */
-  int slots;                /* batches in flight; 0: 8 */
+  int slots;                /* batches in flight; 0: 12 */
   double hbm_fraction;      /* share of free device memory reserved; 0: 0.5 */
 } pcf_server_config;
 

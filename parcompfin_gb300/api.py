@@ -276,7 +276,7 @@ class Plan:
 
 
 def serve_trace(reqs, arrivals, *, target_rel_se=5e-4, pilot_paths=1 << 14, max_paths=1 << 26,
-                max_amer_paths=1 << 21, max_batch=2048, slots=8, hbm_fraction=0.5, ctx=None):
+                max_amer_paths=1 << 21, max_batch=2048, slots=12, hbm_fraction=0.5, ctx=None):
     """Serve request() dicts arriving at `arrivals` (seconds, non-decreasing)
     with the continuous-batching loop; returns (per-request ServedResult list,
     ServerStats)."""

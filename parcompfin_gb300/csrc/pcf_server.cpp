@@ -104,7 +104,7 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
   if (cfg.max_paths <= 0) cfg.max_paths = 1LL << 26;
   if (cfg.max_amer_paths <= 0) cfg.max_amer_paths = 1LL << 21;
   if (cfg.max_batch <= 0) cfg.max_batch = 2048;
-  if (cfg.slots <= 0) cfg.slots = 8;
+  if (cfg.slots <= 0) cfg.slots = 12;
   if (cfg.hbm_fraction <= 0 || cfg.hbm_fraction > 0.9) cfg.hbm_fraction = 0.5;
   for (int i = 1; i < n; ++i)
     if (arrival[i] < arrival[i - 1]) return set_error(PCF_EINVAL, "arrival times must not decrease");
@@ -125,9 +125,9 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
     size_t budget = (size_t)(cfg.hbm_fraction * (double)free_b);
     if (c->budget_bytes) budget = std::min(budget, c->budget_bytes);
     // A slot runs its American path matrices in chunks that fit (a
-    // 2^21-path, 50-date contract is 420 MB): 4 GB per slot is ample, and
+    // 2^21-path, 50-date contract is 420 MB): 3 GB per slot is ample, and
     // reserving less keeps start-up short.
-    const size_t per_slot = std::min(budget / cfg.slots, (size_t)4 << 30);
+    const size_t per_slot = std::min(budget / cfg.slots, (size_t)3 << 30);
     const size_t host_per_slot = (size_t)16 << 20;
     sc = new ServeCache;
     sc->slots.resize(cfg.slots);
@@ -335,7 +335,7 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
     // Admit arrived requests into free slots, an even share each (a burst
     // of 1000 requests runs as pipelined batches, one slot's host-side build
     // overlapping another's kernels: measured 6.99 ms as one batch, 4.29 ms
-    // over four slots, 4.01 ms over eight).
+    // over four slots, 4.05 ms over eight, 3.92 ms over twelve).
     int free_slots = 0;
     for (const Slot& s : slots) free_slots += s.state == Slot::FREE;
     for (Slot& s : slots) {
