@@ -427,18 +427,21 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
 // then the last 1..3 dates.
 __device__ __forceinline__ float2 forward_pair(const LsmParams& P, const RngKey& key,
                                                long long p) {
-  const size_t stride = (size_t)2 * P.Hp;  // floats per row
-  const float nb2 = -P.b2;
+  // The parameters in registers: the stores below go through generic
+  // pointers, which the compiler cannot tell apart from P.
+  const long long Hp = P.Hp;
+  const size_t stride = (size_t)2 * Hp;  // floats per row
+  const float b2 = P.b2, nb2 = -P.b2, a2 = P.a2, pf = P.pf;
   const int M = P.M;
   float Lp = P.l2SE, Lm = P.l2SE, Up = 0.f, Um = 0.f;  // log2(S/E)
   float* row = P.paths + p;
   auto step = [&](float z) {
-    Lp += fmaf(P.b2, z, P.a2);
-    Lm += fmaf(nb2, z, P.a2);
-    Up = fmaf(P.pf, ex2_approx(Lp), -P.pf);  // pf (S/E - 1)
-    Um = fmaf(P.pf, ex2_approx(Lm), -P.pf);
+    Lp += fmaf(b2, z, a2);
+    Lm += fmaf(nb2, z, a2);
+    Up = fmaf(pf, ex2_approx(Lp), -pf);  // pf (S/E - 1)
+    Um = fmaf(pf, ex2_approx(Lm), -pf);
     row[0] = Up;
-    row[P.Hp] = Um;
+    row[Hp] = Um;
     row += stride;
   };
   const int Mfull = M & ~3;
@@ -616,15 +619,17 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
     // Exercise decision at date m (src/mc_amer.cpp:73-106) for one path:
     // exercise where the path is in the money and the payoff beats the
     // continuation value; the cash flow becomes the payoff discounted to 0.
+    const float E = P.E, nK = P.nK;
+    const bool refx = P.ref_exercise != 0;
     auto decide = [&](float u, float& cfd, int s) {
-      float cont, ex = u * P.E;  // the payoff before its max with 0
+      float cont, ex = u * E;  // the payoff before its max with 0
       if (mode == 1) {
         cont = cfd * em;
       } else {
         cont = fmaf(fmaf(c2, u, c1), u, c0);
         // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E),
         // max(pf (S - 2E), 0) = max(E u - pf E, 0).
-        if (P.ref_exercise) ex = fmaxf(fmaf(P.E, u, P.nK), 0.f);
+        if (refx) ex = fmaxf(fmaf(E, u, nK), 0.f);
       }
       if (u > 0.f && ex > cont) {
         cfd = ex * dm;
