@@ -28,8 +28,8 @@ namespace {
 
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-int build_request(pcf_ctx* c, const pcf_mc_request& q, int idx, McContract& k,
-                  std::vector<float>& fb, double& mu_g, double& disc) {
+int build_request(const pcf_mc_request& q, int idx, McContract& k, std::vector<float>& fb,
+                  double& mu_g, double& disc) {
   int st = check_common(q.method == PCF_METHOD_BASKET && q.basket_S0 ? 1.0 : q.S0, q.E, q.r,
                         q.sigma, q.T, q.N, q.payoff_fun);
   if (st) return set_error(st, "request %d: %s", idx, pcf_last_error());
@@ -123,7 +123,7 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
     }
     const int gi = m == PCF_METHOD_BASKET ? 2 + basket_class(reqs[i].assets) : m;
     McContract k;
-    st = build_request(c, reqs[i], i, k, g[gi].fb, p->mu_g[i], p->disc[i]);
+    st = build_request(reqs[i], i, k, g[gi].fb, p->mu_g[i], p->disc[i]);
     if (st) {
       delete p;
       return st;
