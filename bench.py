@@ -7,6 +7,10 @@ Prints one JSON line (rank 0). A step is one pass of the engine over one
 batch of synthetic pricing requests (--workload; parcompfin_gb300/workloads.py
 builds the request sets):
 
+  mixed   (default) the served mixed stream: 1000 requests per step, 30 %
+          European, 20 % basket (2..32 assets), 30 % Asian, 20 % American put,
+          each priced to a 5e-4 relative standard error with its control
+          variate (path counts from an untimed pilot).
   eur     European call S0=K=100 r=.05 sigma=.2 T=1 (mc_eur,
           src/mc_eur.cpp:5-27), 2^28 paths per step.
   asia    Asian book: 256 Asian calls, M in {12,52,252}, N log-uniform in
@@ -18,12 +22,15 @@ builds the request sets):
           (mc_amer, src/mc_amer.cpp:5-114).
   binom   binomial book: 1024 closed-binomial contracts, N uneven in 1e3..2e5
           (binom_embar, src/binom_embar.cpp:5-50), reference rounding order.
+  amerbatch  64 American puts of 2^16 paths and 50 dates in one cluster launch
+          (the mixed stream's American distribution).
 
 value         units/s with the request tables already on the device, timed with
               CUDA events on the engine's stream around each step, L2 flushed
               between steps (outside the events).
 e2e           the same units/s through the public C ABI from host parameters to
-              host results (copies included), wall clock.
+              host results (copies included), wall clock; for the mixed stream
+              the serving loop (pcf_serve_trace), its pilot included.
 roofline      the dominant kernel against its bound (SFU for the path
               generators, HBM for the LSM path matrix).
 cpu_baseline  the reference's OpenMP code on all host cores (oracle/_ref where
