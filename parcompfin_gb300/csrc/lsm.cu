@@ -7,14 +7,18 @@
 // date (src/mc_amer_mpi.cpp:82-131). Here the same exchange runs between the
 // CTAs of one launch, once per exercise date.
 //
-// Two launch forms share one body (lsm_body):
+// Launch forms (the first three share one body, lsm_body):
 //   cooperative  one contract per launch, at most one 512-thread block per
 //                SM (pcf_mc_amer, and batch contracts too large for a
 //                cluster). Blocks exchange their partial sums through global
 //                memory and a bounded group barrier;
 //   cluster      many contracts per launch, one thread-block cluster per
 //                contract (pcf_plan_*). CTAs write their partial sums into
-//                every peer's shared memory and signal the peer's mbarrier.
+//                every peer's shared memory and signal the peer's mbarrier;
+//   cooperative grid of clusters  one large contract: the cluster exchange,
+//                then only the cluster leaders meet in global memory;
+//   streaming    one contract whose per-block slice exceeds shared memory
+//                (lsm_stream_kernel): per-path state in device memory.
 // Phases:
 //   forward   each thread generates its antithetic pairs (path p takes +z,
 //             path p + H takes -z, as pathsfinder pairs them) and writes the
@@ -31,15 +35,16 @@
 //             warp's eight sums in eight lanes; after one block barrier a
 //             single warp adds the warp partials and then all CTAs' partials
 //             in double-float, in a fixed order (every CTA gets the same
-//             bits), widens them to FP64, solves the normal equations and
+//             bits), solves the normal equations in double-float and
 //             publishes the coefficients before a second block barrier;
 //   final     discounted cash flows and the martingale control variate are
 //             averaged over antithetic pairs and reduced with the
 //             deterministic last-block finaliser (cooperative launch) or
 //             through distributed shared memory (cluster launch).
 // Per-path state stays in shared memory for the whole sweep: the cash flow
-// discounted to time 0 (so a date's regression target is one multiply by the
-// date's growth factor) and the exercise date (8 bits where M <= 255). The
+// discounted to time 0 (a date's regression target is that times the date's
+// growth factor, which multiplies the date's three y sums once) and the
+// exercise date (8 bits where M <= 255). The
 // regression basis is {1, u, u^2} with u = pf (S - E)/E: the reference's S - E
 // rescaled (and negated for a put), the same fitted values in exact
 // arithmetic. With u stored, a path is in the money where u > 0 and its
