@@ -12,9 +12,11 @@
 // item. The last item of a contract to finish sums that contract's partials
 // in item order and widens to FP64, so results do not depend on scheduling.
 //
-// The kernels are issue-bound (Philox + Box-Muller + GBM is ~50 FP32/INT
-// instructions against 3 SFU operations per path), so the control-variate
-// sums are compiled in only when a launch asks for them (CV template flag).
+// The kernels are issue-bound (a European path is ~31 FP32/INT instructions,
+// two thirds of them Philox and Box-Muller, against 3 SFU operations), so the
+// control-variate sums are compiled in only when a launch asks for them (CV
+// template flag). Baskets of 17 to 64 assets run mc_basket_tc_kernel, which
+// multiplies the normals by the correlation factor on the tensor cores.
 //
 // Reference loops these kernels replace:
 //   European  src/mc_eur.cpp:22-26,  src/mc_eur_omp.cpp:24-27
