@@ -59,6 +59,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L2_FLUSH_BYTES = 256 << 20  # > the 129 MB L2 of a GB300
+# The cache policy, stated in both arms' config (the same words, so that the
+# two arms' configs compare equal).
+L2_POLICY = ("GPU arm: L2 flushed between steps by a 256 MiB write outside the step's CUDA "
+             "events; CPU arm: no device cache")
 
 
 def _sfu_roofline(sfu_per_unit, units, ms, sms, sm_mhz):
@@ -250,7 +254,29 @@ class BasketWorkload:
 
     def finish(self, ctx):
         r = self.plan.results()
+        self.last_results = r
         return {"prices_cv": [x.price_cv for x in r]}
+
+    def reference_check(self, threads):
+        """Error of each contract against the FP64 harness (the oracle's twin
+        on the identical Philox draws, the same Cholesky factor), all five
+        moment sums, at the full 2^22 paths."""
+        import numpy as np
+        from oracle import loader
+        orc = loader.load()
+        per = []
+        for i, (c, r) in enumerate(zip(self.cs, self.last_results)):
+            d = c["assets"]
+            L = np.linalg.cholesky(np.array(c["corr"])).ravel()
+            s = (C.c_double * 5)()
+            A = C.c_double * d
+            orc.twin_mc_basket(d, A(*c["basket_S0"]), A(*c["basket_sigma"]),
+                               (C.c_double * (d * d))(*L), c["r"], c["T"], math.sqrt(c["T"]),
+                               c["E"], c["N"], 1, 11, self.reqs[i]["stream"], s)
+            err = max(abs(a - b) / abs(b) for a, b in zip(r.sums, s) if b != 0)
+            per.append({"assets": d, "max_rel_err_moments": err})
+        return {"fp64_harness": per,
+                "fp64_harness_max_rel_err": max(x["max_rel_err_moments"] for x in per)}
 
     e2e = EurWorkload.e2e
 
@@ -356,12 +382,10 @@ class LsmWorkload:
             ref(100.0, 100.0, 0.05, 0.3, 1.0, n, self.M, -1.0, threads, 1)
         else:
             kind = "port"
-            orc.ref_mc_amer(100.0, 100.0, 0.05, 0.3, 1.0, n, self.M, -1.0, 1)
-            threads = 1
+            orc.ref_mc_amer_omp(100.0, 100.0, 0.05, 0.3, 1.0, n, self.M, -1.0, 1, threads)
         dt = time.perf_counter() - t0
         return {"value": n / dt, "unit": self.unit, "cores": threads, "kind": kind,
-                "sample": f"{'mc_amer_omp' if ref is not None else 'mc_amer (serial port)'} on "
-                          f"{n} paths, 50 dates, {dt:.2f} s"}
+                "sample": f"mc_amer_omp on {n} paths, 50 dates, {threads} threads, {dt:.2f} s"}
 
 
 class BinomWorkload:
@@ -462,22 +486,21 @@ class MixedWorkload:
         return pcf.request("amer", s["S0"], s["E"], s["r"], s["sigma"], s["T"], N or 2, "put",
                            M=s["M"], **kw)
 
-    def setup(self, ctx):
-        import parcompfin_gb300 as pcf
-        # Pilot (outside the timed region): each request's path count at the
-        # target standard error, for the control-variate estimator (the engine)
-        # and the plain one (the one-contract-per-launch baseline).
-        pilot = [dict(q, N=(1 << 14)) for q in self.base]
-        res = pcf.price_batch(pilot, ctx=ctx)
+    PILOT = 1 << 14
+
+    def _sizes(self, pilot):
+        """Path counts at the target relative standard error from pilot
+        estimates [(se_cv, price_cv, se_plain, price_plain)] at PILOT paths:
+        the control-variate estimator for the engine, the plain one for the
+        one-contract-per-launch baseline. American: [2^16, 2^21], even."""
+        n0 = self.PILOT
+        def need(se, price):
+            if not (se > 0 and price > 0):
+                return n0
+            return int(min(1 << 40, max(n0, 1.05 * se * se * n0 / (self.TARGET * price) ** 2)))
         self.N, self.N_plain = [], []
-        for q, r in zip(self.base, res):
-            n0 = 1 << 14
-            def need(se, price):
-                if not (se > 0 and price > 0):
-                    return n0
-                return int(min(1 << 40, max(n0, 1.05 * se * se * n0 / (self.TARGET * price) ** 2)))
-            n_cv = need(r.std_error_cv, abs(r.price_cv))
-            n_pl = need(r.std_error_plain, abs(r.price_plain))
+        for q, (se_cv, p_cv, se_pl, p_pl) in zip(self.base, pilot):
+            n_cv, n_pl = need(se_cv, abs(p_cv)), need(se_pl, abs(p_pl))
             if q["method"] == 3:
                 n_cv = min(max(n_cv, 1 << 16), 1 << 21) // 2 * 2
                 n_pl = min(max(n_pl, 1 << 16), 1 << 21) // 2 * 2
@@ -486,19 +509,82 @@ class MixedWorkload:
                 n_pl = min(n_pl, 1 << 28)
             self.N.append(n_cv)
             self.N_plain.append(n_pl)
+
+    def setup(self, ctx):
+        import parcompfin_gb300 as pcf
+        # Pilot (outside the timed region): each request's path count at the
+        # target standard error.
+        res = pcf.price_batch([dict(q, N=self.PILOT) for q in self.base], ctx=ctx)
+        self._sizes([(r.std_error_cv, r.price_cv, r.std_error_plain, r.price_plain)
+                     for r in res])
         self.main = [dict(q, N=n) for q, n in zip(self.base, self.N)]
         self.plan = pcf.Plan(self.main, ctx=ctx)
         self.amer_idx = [i for i, q in enumerate(self.main) if q["method"] == 3]
         self.amer_plan = pcf.Plan([self.main[i] for i in self.amer_idx], ctx=ctx)
+
+    def setup_cpu(self, threads):
+        """The reference arm's sizing, without the engine: the same pilot on
+        the oracle's FP64 restatements fed the identical Philox draws (same
+        seeds and streams, PILOT paths), so the path counts are the engine's
+        up to the restatements' FP64 rounding."""
+        from oracle import loader
+        from oracle.served_check import _cv_estimate
+        import numpy as np
+        orc = loader.load()
+        n0 = self.PILOT
+        pilot = []
+        for q, sp in zip(self.base, self.spec):
+            pf, S0, E, r, sig, T = q["payoff_fun"], q["S0"], q["E"], q["r"], q["sigma"], q["T"]
+            s = (C.c_double * 6)()
+            disc, n = math.exp(-r * T), n0
+            if q["method"] == 0:
+                orc.twin_mc_eur(S0, E, r, sig, T, n0, pf, q["seed"], q["stream"], s)
+                mu = S0 * math.exp(r * T)
+            elif q["method"] == 1:
+                orc.twin_mc_asia(S0, E, r, sig, T, n0, q["M"], pf, q["mode"], q["seed"],
+                                 q["stream"], s)
+                w = (C.c_double * (q["M"] + 1))()
+                orc.orc_asian_geo_weights(q["M"], q["mode"], w)
+                mu = orc.orc_geo_weighted_price(S0, E, r, sig, T, q["M"], w, pf, None) / disc
+            elif q["method"] == 2:
+                d = q["assets"]
+                corr = np.full((d, d), q["rho"])
+                np.fill_diagonal(corr, 1.0)
+                L = np.linalg.cholesky(corr).ravel()
+                A = C.c_double * d
+                sg = A(*sp["basket_sigma"])
+                s0 = A(*([S0] * d))
+                orc.twin_mc_basket(d, s0, sg, (C.c_double * (d * d))(*L), r, T, math.sqrt(T), E,
+                                   n0, pf, q["seed"], q["stream"], s)
+                mu = orc.orc_geo_basket_price(d, s0, sg, (C.c_double * (d * d))(*corr.ravel()), r,
+                                              T, math.sqrt(T), E, pf, None) / disc
+            else:
+                orc.twin_mc_amer(S0, E, r, sig, T, n0, q["M"], pf, q["mode"], q["seed"],
+                                 q["stream"], s)
+                mu, disc, n = orc.orc_bs_price(S0, E, r, sig, T, pf), 1.0, n0 // 2
+            p_cv, se_cv = _cv_estimate(list(s), n, mu, disc)
+            m = s[0] / n
+            se_pl = disc * math.sqrt(max(s[1] / n - m * m, 0.0) / (n - 1))
+            pilot.append((se_cv, p_cv, se_pl, disc * m))
+        self._sizes(pilot)
 
     def step(self, ctx):
         self.plan.launch()
 
     def finish(self, ctx):
         res = self.plan.results()
+        self.last_results = res
         rel = sorted(r.std_error / r.price for r in res if r.price > 0 and r.std_error == r.std_error)
         return {"requests": len(res), "median_rel_se": rel[len(rel) // 2], "max_rel_se": rel[-1],
                 "paths_per_step": self.units()}
+
+    def reference_check(self, threads):
+        """The step's prices against the reference's pricers (oracle/served_check.py),
+        on up to 40 requests of each kind."""
+        from oracle import loader, served_check
+        rep = served_check.check(loader.load(), self.main, self.last_results, threads=threads,
+                                 max_per_kind=40)
+        return rep["per_kind"]
 
     def e2e(self, ctx):
         # The C-ABI call of the serving loop on host buffers: the request
@@ -539,8 +625,7 @@ class MixedWorkload:
                             "distribution), 20% American put (LSM, 50 dates, N in 2^16..2^21); "
                             "each priced to a 5e-4 relative standard error with its control "
                             "variate",
-                "requests_per_step": self.R, "kinds": kinds, "target_rel_se": self.TARGET,
-                "paths_per_step": self.units() if hasattr(self, "N") else None}
+                "requests_per_step": self.R, "kinds": kinds, "target_rel_se": self.TARGET}
 
     def roofline(self, ms, sms, mhz, peaks):
         import torch
@@ -614,59 +699,100 @@ class MixedWorkload:
                          "5e-4 relative standard error (American capped at 2^21)"}
         return {"served": served, "plain_gpu": plain}
 
-    def cpu_reference(self, threads, budget_s):
+    def cpu_reference(self, threads, budget_s, step=0):
+        """The reference's OpenMP pricers on the host cores, for the same
+        requests at the same path counts as the engine's step, extrapolated
+        from a timed sample: each sampled request runs at its own parameters
+        on a reduced path count n, its time per path gives the per-kind cost
+        model (European per path, Asian per path-step, basket per path as a
+        function of d, American per path-date), and the model prices every
+        request at its N. A linear model from small n leaves out the cache
+        misses of large N, so it understates the CPU time. The basket uses the
+        oracle's FP64 restatement (the reference's needs Eigen and Boost)."""
+        import numpy as np
         from oracle import loader
         orc = loader.load()
         refs = {k: loader.load_ref(k) for k in ("mc_eur_omp", "mc_asia_omp", "mc_amer_omp")}
         kind = "reference" if all(refs.values()) else "port"
-        t0 = time.perf_counter()
-        paths = 0
-        done = 0
-        for s in self.spec:
-            n = 1 << 15 if s["kind"] in ("eur", "basket") else 1 << 13
-            if s["kind"] == "eur":
-                if refs["mc_eur_omp"]:
-                    refs["mc_eur_omp"](s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, 0, 1.0,
-                                       threads, 1)
+        by = {k: [i for i, sp in enumerate(self.spec) if sp["kind"] == k]
+              for k in ("eur", "asia", "basket", "amer")}
+        # Per step a rotating, bounded sample of each kind.
+        per = {"eur": 6, "asia": 8, "basket": 8, "amer": 3}
+        if budget_s >= 5:
+            per = {k: 3 * v for k, v in per.items()}
+        samples = {}
+        for k, idx in by.items():
+            n = min(per[k], len(idx))
+            off = (step * n) % max(1, len(idx))
+            samples[k] = [idx[(off + j) % len(idx)] for j in range(n)]
+        cost = {k: [] for k in by}  # (request, seconds per unit)
+        t_all = time.perf_counter()
+        for k in ("eur", "asia", "basket", "amer"):
+            for i in samples[k]:
+                sp, q = self.spec[i], self.base[i]
+                S0, E, r, sig, T = sp["S0"], sp["E"], sp["r"], sp["sigma"], sp["T"]
+                if k == "eur":
+                    n = 1 << 19
+                    t0 = time.perf_counter()
+                    if refs["mc_eur_omp"]:
+                        refs["mc_eur_omp"](S0, E, r, sig, T, n, 0, 1.0, threads, 1)
+                    else:
+                        orc.ref_mc_eur_omp(S0, E, r, sig, T, n, 1.0, 1, threads)
+                    units = n
+                elif k == "asia":
+                    n = max(2000, int(4e6 / sp["M"]))
+                    t0 = time.perf_counter()
+                    if refs["mc_asia_omp"]:
+                        refs["mc_asia_omp"](S0, E, r, sig, T, n, sp["M"], 1.0, threads, 1)
+                    else:
+                        orc.ref_mc_asia_omp(S0, E, r, sig, T, n, sp["M"], 1.0, 1, threads)
+                    units = n * sp["M"]
+                elif k == "basket":
+                    d, n = sp["assets"], 1 << 14
+                    corr = np.full((d, d), sp["rho"])
+                    np.fill_diagonal(corr, 1.0)
+                    L = np.linalg.cholesky(corr).ravel()
+                    A = C.c_double * d
+                    sums = (C.c_double * 5)()
+                    t0 = time.perf_counter()
+                    orc.twin_mc_basket(d, A(*([S0] * d)), A(*sp["basket_sigma"]),
+                                       (C.c_double * (d * d))(*L), r, T, math.sqrt(T), E, n, 1,
+                                       1, 0, sums)
+                    units = n * (d * d + 8 * d + 20)
                 else:
-                    orc.ref_mc_eur_omp(s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, 1.0, 1,
-                                       threads)
-            elif s["kind"] == "asia":
-                if refs["mc_asia_omp"]:
-                    refs["mc_asia_omp"](s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"], 1.0,
-                                        threads, 1)
-                else:
-                    orc.ref_mc_asia_omp(s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"], 1.0,
-                                        1, threads)
-            elif s["kind"] == "basket":
-                # No Eigen/Boost build of the reference basket here: the oracle's
-                # FP64 restatement on all cores stands in.
-                import numpy as np
-                d = s["assets"]
-                corr = np.full((d, d), s["rho"])
-                np.fill_diagonal(corr, 1.0)
-                L = np.linalg.cholesky(corr).ravel()
-                A = C.c_double * d
-                sums = (C.c_double * 5)()
-                orc.twin_mc_basket(d, A(*([s["S0"]] * d)), A(*s["basket_sigma"]),
-                                   (C.c_double * (d * d))(*L), s["r"], s["T"], math.sqrt(s["T"]),
-                                   s["E"], n, 1, 1, 0, sums)
-            else:
-                if refs["mc_amer_omp"]:
-                    refs["mc_amer_omp"](s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"],
-                                        -1.0, threads, 1)
-                else:
-                    orc.ref_mc_amer(s["S0"], s["E"], s["r"], s["sigma"], s["T"], n, s["M"], -1.0, 1)
-            paths += n
-            done += 1
-            if time.perf_counter() - t0 > budget_s:
-                break
-        dt = time.perf_counter() - t0
-        return {"value": paths / dt, "unit": self.unit, "cores": threads, "kind": kind,
-                "ms_per_step": 1e3 * dt,
-                "sample": f"the reference's OpenMP pricers (basket: oracle restatement) on the first "
-                          f"{done} requests of the mix, 2^15 paths (European, basket) or 2^13 "
-                          f"(Asian, American) each: {paths} paths in {dt:.2f} s"}
+                    n = 1 << 14
+                    t0 = time.perf_counter()
+                    if refs["mc_amer_omp"]:
+                        refs["mc_amer_omp"](S0, E, r, sig, T, n, sp["M"], -1.0, threads, 1)
+                    else:
+                        orc.ref_mc_amer_omp(S0, E, r, sig, T, n, sp["M"], -1.0, 1, threads)
+                    units = n * sp["M"]
+                cost[k].append(max(time.perf_counter() - t0, 1e-9) / units)
+        sampled = time.perf_counter() - t_all
+        unit_cost = {k: statistics.median(v) for k, v in cost.items() if v}
+
+        def units_of(i, N):
+            sp = self.spec[i]
+            if sp["kind"] == "eur":
+                return N
+            if sp["kind"] == "basket":
+                d = sp["assets"]
+                return N * (d * d + 8 * d + 20)
+            return N * sp["M"]
+
+        secs = {k: sum(unit_cost[k] * units_of(i, self.N[i]) for i in idx) for k, idx in by.items()}
+        total = sum(secs.values())
+        paths = float(sum(self.N))
+        return {"value": paths / total, "unit": self.unit, "cores": threads, "kind": kind,
+                "ms_per_step": 1e3 * total, "contracts_per_s": len(self.N) / total,
+                "extrapolated": True,
+                "seconds_by_kind": {k: round(v, 3) for k, v in secs.items()},
+                "sample": f"the reference's OpenMP pricers (mc_eur_omp, mc_asia_omp, mc_amer_omp; "
+                          f"basket: the oracle's FP64 restatement) on the host cores, timed on "
+                          f"{sum(len(v) for v in samples.values())} requests of the mix at their "
+                          f"own parameters and reduced path counts ({sampled:.1f} s), then "
+                          f"extrapolated to the same {len(self.N)} requests at the engine's path "
+                          f"counts ({paths:.3e} paths): {total:.2f} s per step (extrapolated)"}
 
 
 class AmerBatchWorkload:
@@ -796,23 +922,30 @@ def run_reference(args, wl_cls):
         return
     threads = os.cpu_count() or 1
     wl = wl_cls(0)
-    vals, sample = [], None
+    if hasattr(wl, "setup_cpu"):
+        wl.setup_cpu(threads)
+    vals, ms_vals, sample = [], [], None
     for i in range(args.warmup + args.steps):
-        r = wl.cpu_reference(threads, budget_s=2.0)
+        if hasattr(wl, "setup_cpu"):
+            r = wl.cpu_reference(threads, budget_s=2.0, step=i)
+        else:
+            r = wl.cpu_reference(threads, budget_s=2.0)
         if i >= args.warmup:
             vals.append(r["value"])
+            ms_vals.append(r.get("ms_per_step", 1e3 * wl.units() / r["value"]))
             sample = r
     value = statistics.median(vals)
-    ms_step = sample.get("ms_per_step")
-    if ms_step is None:
-        ms_step = 1e3 * wl.units() / value
+    ms_step = statistics.median(ms_vals)
     line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": wl.config(),
+            "config": dict(wl.config(), l2=L2_POLICY),
+            "paths_per_step": wl.units() if wl.unit == "paths/s" else None,
             "cpu_baseline": {"value": value, "unit": wl.unit, "cores": sample["cores"],
-                             "kind": sample["kind"], "sample": sample["sample"]},
+                             "kind": sample["kind"], "sample": sample["sample"],
+                             **{k: sample[k] for k in ("extrapolated", "contracts_per_s",
+                                                       "seconds_by_kind") if k in sample}},
             "e2e": {"value": value, "unit": wl.unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -900,9 +1033,9 @@ def run_ours(args, wl_cls):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 paths, f64 sums" if wl.name != "binom" else "f64", "data": "synthetic",
-        "config": dict(wl.config(), l2="flushed: 256 MiB write between steps, outside the "
-                                       "per-step CUDA events",
-                       wall_ms_per_step=1e3 * t_wall / args.steps),
+        "config": dict(wl.config(), l2=L2_POLICY),
+        "wall_ms_per_step": 1e3 * t_wall / args.steps,
+        "paths_per_step": wl.units() if wl.unit == "paths/s" else None,
         "roofline": roof,
         "e2e": {"value": e2e_units / (e2e_med * 1e-3) if e2e_ms else None, "unit": wl.unit,
                 "h2d_bytes_per_step": io[0], "d2h_bytes_per_step": io[1], "ms_per_step": e2e_med},
@@ -918,11 +1051,18 @@ def run_ours(args, wl_cls):
             line["plain_gpu"]["engine_over_plain_contracts"] = (
                 line["contracts_per_s"] / line["plain_gpu"]["contracts_per_s"])
     if not args.no_cpu:
+        threads = os.cpu_count() or 1
         try:
-            line["cpu_baseline"] = wl.cpu_reference(os.cpu_count() or 1, budget_s=10.0)
-            line["cpu_baseline"].pop("ms_per_step", None)
+            line["cpu_baseline"] = wl.cpu_reference(threads, budget_s=10.0)
         except Exception as e:  # noqa: BLE001
             line["cpu_baseline"] = {"error": repr(e)}
+        if hasattr(wl, "reference_check"):
+            # The CPU leg is where the oracle runs, as the checker of the
+            # step's results (never inside the timed region).
+            try:
+                line["check"]["vs_reference"] = wl.reference_check(threads)
+            except Exception as e:  # noqa: BLE001
+                line["check"]["vs_reference"] = {"error": repr(e)}
     print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:

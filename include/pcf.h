@@ -134,11 +134,44 @@ PCF_API int pcf_mc_basket(pcf_ctx* ctx, int d, const double* S0, const double* s
  * ref_exercise = 0 exercises at payoff(S) (correct LSM); 1 reproduces the
  * reference's exercise value payoff(S - E, E) of src/mc_amer.cpp:100, which
  * makes its puts far too high. price = max(payoff(S0), mean discounted cash
- * flow) as src/mc_amer.cpp:113. Control variate: the discounted European
- * payoff at T (mean = Black-Scholes). */
+ * flow) as src/mc_amer.cpp:113. Control variate (a martingale, mean =
+ * Black-Scholes): with ref_exercise = 0, the European price at the path's
+ * exercise date tau discounted to time 0 (the discounted payoff at T for a
+ * path held to T); with ref_exercise = 1, whose exercise value does not
+ * identify S_tau, the discounted European payoff at T. */
 PCF_API int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
                         long long N, int M, int payoff_fun, int ref_exercise,
                         unsigned long long seed, int use_cv, pcf_mc_result* out);
+
+/* pcf_mc_amer (use_cv = 1) plus an audit record of the sweep, for checking
+ * the GPU's exercise policy against an FP64 re-run on the host. Any of the
+ * buffers may be NULL:
+ *   coef[M*4]  per date d (index d = 1..M-1; index 0 unused) {mode, c0, c1,
+ *              c2}: mode 0 skipped (no in-the-money path, or a singular
+ *              system), 1 at most two in-the-money paths, 2 the regression
+ *              continuation value c0 + c1 u + c2 u^2 with
+ *              u = payoff_fun (S - E) / E;
+ *   sums[M*8]  the regression sums of date d as the solve saw them
+ *              {n, sum u, u^2, u^3, u^4, y, y u, y u^2}, y the cash flow
+ *              discounted to date d;
+ *   tau[N]     each path's exercise date (M: held to T); paths p and
+ *              p + N/2 are antithetic;
+ *   u[M*N]     the FP32 path matrix: row m-1 holds u at date m.
+ * Has no counterpart in the reference. */
+PCF_API int pcf_mc_amer_audit(pcf_ctx* ctx, double S0, double E, double r, double sigma,
+                              double T, long long N, int M, int payoff_fun, int ref_exercise,
+                              unsigned long long seed, pcf_mc_result* out, float* coef,
+                              double* sums, unsigned short* tau, float* u);
+
+/* Test hook for the failure paths (no counterpart in the reference): while
+ * extra_arrivals > 0, the cooperative group barriers of pcf_mc_amer (plain
+ * cooperative grid only: the cluster forms are not used while it is set) and
+ * pcf_binom_vanilla wait for extra_arrivals blocks more than the grid holds,
+ * so they cannot complete, and give up after poll_limit polls; the call then
+ * returns PCF_ETIMEOUT. Waits on bulk copies keep their full limit, so no
+ * block leaves with a copy in flight. extra_arrivals = 0 restores normal
+ * operation; the counters are reset by every call. */
+PCF_API int pcf_ctx_set_test_barrier(pcf_ctx* ctx, unsigned extra_arrivals, unsigned poll_limit);
 
 /* European option by the closed binomial sum on the reference's
  * beta-parametrised lattice (u = beta + sqrt(beta^2 - 1), d = 1/u).
@@ -185,7 +218,9 @@ PCF_API int pcf_binom_vanilla(pcf_ctx* ctx, double S0, double E, double r, doubl
  *     GPU that loads it, held until the process exits). N is limited to 2^30
  *     paths; larger N returns PCF_EINVAL.
  *   - The first call on each device looks up that array's device address
- *     and the SM count; make that first call before any stream capture.
+ *     (cudaGetSymbolAddress, with that device current) and keeps it for the
+ *     life of the process; make that first call before any stream capture.
+ *     After cudaDeviceReset the kept address is stale: restart the process.
  *   - All calls share the array, so calls whose kernels overlap on the GPU
  *     (concurrent streams, other host threads) race and must be serialised
  *     by the caller.

@@ -8,9 +8,11 @@
 # sources are read in place and never copied. mc_eur_multi* needs Eigen and
 # Boost, which this image does not have, so it is not built.
 #
-# Usage: sh oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: sh oracle/build_ref.sh REFERENCE_ROOT
+#        (or PCF_REFERENCE_ROOT=... sh oracle/build_ref.sh)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$PCF_REFERENCE_ROOT}
+[ -n "$REF" ] || { echo "usage: $0 REFERENCE_ROOT"; exit 2; }
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF/src" ] || { echo "reference not found at $REF; skipping"; exit 0; }

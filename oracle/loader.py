@@ -34,6 +34,8 @@ SIGS = {
     "ref_mc_asia": (_D, [_D, _D, _D, _D, _D, _I, _I, _D, _U32]),
     "ref_mc_asia_omp": (_D, [_D, _D, _D, _D, _D, _I, _I, _D, _U32, _I]),
     "ref_mc_amer": (_D, [_D, _D, _D, _D, _D, _I, _I, _D, _U32]),
+    "ref_mc_amer_omp": (_D, [_D, _D, _D, _D, _D, _I, _I, _D, _U32, _I]),
+    "ref_mc_asia_omp_stats": (None, [_D, _D, _D, _D, _D, _I, _I, _D, _U32, _I, _PD]),
     "ref_binom_embar": (_D, [_D, _D, _D, _D, _D, _I, _D]),
     "ref_binom_embar_omp": (_D, [_D, _D, _D, _D, _D, _I, _D, _I]),
     "ref_binom_embar_window": (_D, [_D, _D, _D, _D, _D, _I, _D, _I, _I]),
@@ -45,6 +47,9 @@ SIGS = {
     "twin_mc_asia": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _I, _U64, _U32, _PD]),
     "twin_mc_basket": (None, [_I, _PD, _PD, _PD, _D, _D, _D, _D, _I64, _I, _U64, _U32, _PD]),
     "twin_mc_amer": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _I, _U64, _U32, _PD]),
+    "twin_mc_amer_audit": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _I, _U64, _U32,
+                                  C.POINTER(C.c_float), _PD, C.POINTER(C.c_uint16),
+                                  C.POINTER(C.c_float), _PD, _PD]),
 }
 
 
@@ -62,9 +67,13 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_ref(reference_root: str = "/root/reference") -> bool:
-    """Compile the reference's own sources into _ref/ when they are present."""
-    if not os.path.isdir(os.path.join(reference_root, "src")):
+def build_ref(reference_root: str | None = None) -> bool:
+    """Compile the reference's own sources into _ref/ when they are present.
+
+    The location is the argument, else the PCF_REFERENCE_ROOT environment
+    variable; with neither, or no sources there, nothing is built."""
+    reference_root = reference_root or os.environ.get("PCF_REFERENCE_ROOT", "")
+    if not reference_root or not os.path.isdir(os.path.join(reference_root, "src")):
         return False
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), reference_root], check=True,
                    capture_output=True)

@@ -475,6 +475,124 @@ ORC_EXPORT double ref_binom_vanilla_eur(double S0, double E, double r, double si
   return v[0];
 }
 
+/* src/mc_amer_omp.cpp:5-117, the OpenMP build of mc_amer: the paths come
+ * from pathsfinder seeded with time() + 100 * threads (include/common.h:192,
+ * `parallel` = threads); the regression sums are an OpenMP reduction with
+ * schedule(dynamic,1000); the <= 2 in-the-money branch exercises where
+ * x = S - E beats y and records x as the exercise value (src/mc_amer_omp.cpp:
+ * 72-81, unlike the serial build); the exercise update loop is serial; the
+ * final mean sums the paths whose exercise date is not 0. With threads = 1
+ * the reductions run in path order, so the result is the reference's bit for
+ * bit. Returns NaN where the reference throws (odd N, det <= 0). */
+ORC_EXPORT double ref_mc_amer_omp(double S0, double E, double r, double sigma, double T, int N,
+                                  int M, double payoff_fun, uint32_t seed, int threads) {
+  if (threads > 0) omp_set_num_threads(threads);
+  const double dt = T / M;
+  const int pf = (int)payoff_fun;
+  double result = 0;
+  std::vector<std::vector<double>> paths;
+  if (!pathsfinder(S0, r, sigma, T, N, M, seed + 100u * (uint32_t)threads, paths)) return NAN;
+  std::vector<double> exercise_when((size_t)N, (double)M);
+  std::vector<double> exercise_st((size_t)N);
+  for (int n = 0; n < N; ++n) exercise_st[n] = payoff(paths[M][n], E, pf);
+  for (int m = M - 1; m > 0; --m) {
+    std::vector<double> x((size_t)N, -1), y((size_t)N, -1);
+    double sum_x = 0, sum_x2 = 0, sum_x3 = 0, sum_x4 = 0, sum_y = 0, sum_yx = 0, sum_yx2 = 0;
+    double x_length = 0;
+#pragma omp parallel
+    {
+#pragma omp for schedule(dynamic, 1000) nowait reduction(+ : sum_x, sum_x2, sum_x3, sum_x4, \
+                                                              sum_y, sum_yx, sum_yx2, x_length)
+      for (int n = 0; n < N; ++n) {
+        const double payoff_val = payoff(paths[m][n], E, pf);
+        if (payoff_val > 0) {
+          ++x_length;
+          const double exer = paths[m][n] - E;
+          x[n] = exer;
+          const double cont = exp(-r * dt * (exercise_when[n] - m)) *
+                              payoff(paths[(size_t)exercise_when[n]][n], E, pf);
+          y[n] = cont;
+          sum_x += exer;
+          sum_x2 += exer * exer;
+          sum_x3 += exer * exer * exer;
+          sum_x4 += exer * exer * exer * exer;
+          sum_y += cont;
+          sum_yx += cont * exer;
+          sum_yx2 += cont * exer * exer;
+        }
+      }
+    }
+    if (x_length == 0) continue;
+    if (x_length <= 2) {
+#pragma omp parallel for
+      for (int i = 0; i < N; ++i)
+        if (x[i] > y[i]) {
+          exercise_when[i] = m;
+          exercise_st[i] = x[i];
+        }
+      continue;
+    }
+    const double xTx[3][3] = {{x_length, sum_x, sum_x2}, {sum_x, sum_x2, sum_x3}, {sum_x2, sum_x3, sum_x4}};
+    const double xTy[3] = {sum_y, sum_yx, sum_yx2};
+    double coef[3];
+    if (!solve3_cofactor(xTx, xTy, coef)) return NAN;
+    for (int i = 0; i < N; ++i) {
+      if (x[i] != -1) {
+        const double Y_hat = coef[0] + coef[1] * x[i] + coef[2] * pow(x[i], 2);
+        const double payoff_val = payoff(x[i], E, pf);
+        if (payoff_val > Y_hat) {
+          exercise_when[i] = m;
+          exercise_st[i] = payoff_val;
+        }
+      }
+    }
+  }
+#pragma omp parallel
+  {
+#pragma omp for schedule(dynamic, 1000) nowait reduction(+ : result)
+    for (int n = 0; n < N; ++n)
+      if (exercise_when[n] != 0) result += exp(-r * exercise_when[n] * dt) * exercise_st[n];
+  }
+  return std::max(payoff(S0, E, pf), result / (double)N);
+}
+
+/* The estimator of src/mc_asia_omp.cpp:5-48 (per-thread mt19937 seeded with
+ * time() * (1 + thread), the reference's running sum) with its sample
+ * variance: out = {price, standard error}. The served-price checks compare
+ * the engine's Asian prices with the reference's estimator at a combined
+ * standard error. */
+ORC_EXPORT void ref_mc_asia_omp_stats(double S0, double E, double r, double sigma, double T,
+                                      int N, int M, double payoff_fun, uint32_t seed, int threads,
+                                      double* out) {
+  double s1 = 0, s2 = 0;
+  const int pf = (int)payoff_fun;
+  if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel
+  {
+    const double dt = (double)T / (double)M;
+    const int thr = omp_get_thread_num();
+    std::mt19937 gen;
+    gen.seed(seed * (uint32_t)(1 + thr));
+    std::normal_distribution<> norm{0, sqrt(dt)};
+#pragma omp for nowait schedule(dynamic, 1000) reduction(+ : s1, s2)
+    for (int n = 0; n < N; ++n) {
+      double St = S0, I = 0;
+      for (int m = 0; m < M; ++m) {
+        const double dBi = norm(gen);
+        I += St * (1 + r * dt / 2 + sigma * dBi / 2);
+        St *= exp((r - pow(sigma, 2) / 2) * dt + sigma * dBi);
+      }
+      const double y = payoff(I / (double)M, E, pf);
+      s1 += y;
+      s2 += y * y;
+    }
+  }
+  const double disc = exp(-r * T), mean = s1 / N;
+  const double var = N > 1 ? std::max(0.0, (s2 - N * mean * mean) / (N - 1)) : 0.0;
+  out[0] = disc * mean;
+  out[1] = disc * sqrt(var / N);
+}
+
 /* src/binom_vanilla_amer.cpp:5-40 (backward induction with early exercise). */
 ORC_EXPORT double ref_binom_vanilla_amer(double S0, double E, double r, double sigma, double T,
                                          int N, double payoff_fun) {
@@ -688,4 +806,364 @@ ORC_EXPORT void twin_mc_amer(double S0, double E, double r, double sigma, double
   }
   for (int k = 0; k < 5; ++k) out[k] = s[k];
   out[5] = singular;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3. Audit of a GPU Longstaff-Schwartz sweep (pcf_mc_amer_audit's record)   */
+/* ------------------------------------------------------------------------ */
+/* Checks the GPU's exercise policy three ways, with the reference's
+ * algorithm (src/mc_amer.cpp:31-113: in-the-money regression on {1, x, x^2},
+ * the <= 2 in-the-money branch, exercise where the exercise value beats the
+ * fitted continuation value) in the GPU's basis u = pf (S - E)/E:
+ *
+ * R1  the GPU's own FP32 path matrix `gu` and coefficients `gcoef`, its
+ *     decision arithmetic replayed in FP32 exactly (the kernel's formulas,
+ *     fmaf included): must reproduce the GPU's exercise dates `gtau` path
+ *     for path. On the same state the regression sums are formed in FP64
+ *     and solved in FP64 (the adjugate of include/common.h:98-141), giving
+ *     the sums' and the fitted values' errors, and the decisions the FP64
+ *     coefficients would change.
+ * R2  FP64 paths (the twin's Philox draws) with the GPU's coefficients,
+ *     decided in FP64: each decision that differs from the GPU's is checked
+ *     to lie within FP32 rounding of the exercise boundary, i.e. the FP64
+ *     decision function changes sign between the FP64 path value and the
+ *     GPU's FP32 one, or its value at the GPU's path is within the FP32
+ *     evaluation error of the kernel's formula.
+ * R3  the independent FP64 twin (its own FP64 regressions), compared with
+ *     the GPU's policy and price.
+ *
+ * rep[] (doubles): 0 R1 exercise-date mismatches, 1 R1 mode mismatches,
+ * 2 max relative error of the GPU's regression sums, 3 max fitted-value error
+ * of the GPU's coefficients against the FP64 regression of the same state (/E),
+ * 4 the same for the solve alone (FP64 solve of the GPU's sums), 5 decisions
+ * the FP64 coefficients would change, 6 their largest margin (/E),
+ * 7 relative difference of sum y (GPU vs FP64 moments of the R1 state),
+ * 8 the same for sum g, 9 max |u_gpu - u_fp64|, 10 R2 decision flips,
+ * 11 R2 flips not within FP32 rounding of the boundary, 12 R2 exercise dates
+ * differing from the GPU's, 13 relative difference of sum y (R2 vs GPU),
+ * 14 relative difference of the GPU's sum y and the FP64 value of its own
+ * exercise dates on FP64 paths, 15 R3 exercise dates differing from the
+ * GPU's, 16 relative difference of sum y (R3 vs GPU), 17 the same for sum g,
+ * 18 largest |exercise - continuation| / E of an R2 flip, 19 regression dates,
+ * 20 in-the-money path-dates of the regression dates, 21 R4 exercise dates
+ * differing from the GPU's, 22 relative difference of sum y (R4 vs GPU),
+ * 23 exercise dates differing between R4 and R3, 24 relative difference of
+ * sum y (R3 vs R4).
+ *
+ * R4  the GPU's FP32 path matrix with FP64 regressions and FP64 decisions
+ *     (no replay): R4 against the GPU isolates the kernel's arithmetic, R3
+ *     against R4 the FP32 representation of the paths alone. */
+namespace {
+struct AmerAuditIn {
+  double S0, E, r, sigma, T;
+  int64_t N;
+  int M, pf, refx;
+};
+
+double rel_diff(double a, double b) { return fabs(a - b) / std::max(fabs(b), 1e-300); }
+
+/* FP64 regression of one date; returns the mode as the kernel defines it
+ * (0 skip, 1 at most two in-the-money paths, 2 regression). */
+int solve_mode(const double a[8], double coef[3]) {
+  coef[0] = coef[1] = coef[2] = 0;
+  if (a[0] == 0) return 0;
+  if (a[0] <= 2) return 1;
+  const double xtx[3][3] = {{a[0], a[1], a[2]}, {a[1], a[2], a[3]}, {a[2], a[3], a[4]}};
+  const double xty[3] = {a[5], a[6], a[7]};
+  return solve3_cofactor(xtx, xty, coef) ? 2 : 0;
+}
+}  // namespace
+
+ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, double T,
+                                   int64_t N, int M, int pf, int ref_exercise, uint64_t seed,
+                                   uint32_t stream, const float* gcoef, const double* gsums,
+                                   const uint16_t* gtau, const float* gu, const double* gmom,
+                                   double* rep) {
+  for (int k = 0; k < 25; ++k) rep[k] = 0;
+  const int64_t H = N / 2;
+  const double dtd = T / M;
+  /* The kernel's FP32 constants, made as the host makes them. */
+  std::vector<float> dtf((size_t)M + 1), edtf((size_t)M + 1);
+  for (int k = 0; k <= M; ++k) {
+    dtf[k] = (float)exp(-r * dtd * k);
+    edtf[k] = (float)exp(r * dtd * k);
+  }
+  const float Ef = (float)E, nKf = (float)(-pf * E), pff = (float)pf;
+  const float EdM = Ef * dtf[M];
+  auto U = [&](int m, int64_t n) { return gu[(size_t)(m - 1) * N + n]; };  /* date m */
+
+  /* FP64 paths (the twin's draws), u64 = pf (S/E - 1). */
+  const double sdt = sqrt(dtd), nu_dt = (r - 0.5 * sigma * sigma) * dtd;
+  std::vector<double> S((size_t)(M + 1) * N);
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < H; ++p) {
+    double lp = 0, lm = 0, z[4] = {0, 0, 0, 0};
+    S[p] = S0;
+    S[p + H] = S0;
+    for (int m = 1; m <= M; ++m) {
+      if ((m - 1) % 4 == 0) orc::normals4(seed, stream, 4u, (uint64_t)p, (uint32_t)((m - 1) / 4), z);
+      const double zm = z[(m - 1) % 4];
+      lp += nu_dt + sigma * sdt * zm;
+      lm += nu_dt - sigma * sdt * zm;
+      S[(size_t)m * N + p] = S0 * exp(lp);
+      S[(size_t)m * N + p + H] = S0 * exp(lm);
+    }
+  }
+  auto U64 = [&](int m, int64_t n) { return pf * (S[(size_t)m * N + n] / E - 1.0); };
+  double du = 0;
+#pragma omp parallel for reduction(max : du) schedule(static)
+  for (int64_t n = 0; n < N; ++n)
+    for (int m = 1; m <= M; ++m) du = std::max(du, fabs((double)U(m, n) - U64(m, n)));
+  rep[9] = du;
+  std::vector<double> disc((size_t)M + 1);
+  for (int k = 0; k <= M; ++k) disc[k] = exp(-r * dtd * k);
+
+  /* ---- R1: the GPU's paths and coefficients, its FP32 decisions ---- */
+  std::vector<float> cf1((size_t)N);
+  std::vector<int> tau1((size_t)N, M);
+  for (int64_t n = 0; n < N; ++n) cf1[n] = fmaxf(U(M, n), 0.f) * EdM;
+  /* ---- R2: FP64 paths, the GPU's coefficients, FP64 decisions ---- */
+  std::vector<double> cf2((size_t)N);  /* cash flow at tau2 (undiscounted) */
+  std::vector<int> tau2((size_t)N, M);
+  /* ---- R3: the independent FP64 twin ---- */
+  std::vector<double> cf3((size_t)N);
+  std::vector<int> tau3((size_t)N, M);
+  for (int64_t n = 0; n < N; ++n) cf2[n] = cf3[n] = E * std::max(U64(M, n), 0.0);
+  /* ---- R4: the GPU's FP32 paths, FP64 regressions and decisions ---- */
+  std::vector<double> cf4((size_t)N);
+  std::vector<int> tau4((size_t)N, M);
+  for (int64_t n = 0; n < N; ++n) cf4[n] = E * std::max((double)U(M, n), 0.0);
+
+  long long mode_mis = 0, cflips = 0, flips2 = 0, unexpl = 0, rdates = 0, itm_dates = 0;
+  double sum_err = 0, fit_err = 0, fit_err_solve = 0, cmargin = 0, fmargin = 0;
+  for (int m = M - 1; m >= 1; --m) {
+    const int gmode = (int)gcoef[(size_t)m * 4];
+    const float c0 = gcoef[(size_t)m * 4 + 1], c1 = gcoef[(size_t)m * 4 + 2],
+                c2 = gcoef[(size_t)m * 4 + 3];
+    const float dm = dtf[m], em = edtf[m];
+    /* R1 sums in FP64 on the GPU's state. */
+    double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma omp parallel for reduction(+ : a[:8]) schedule(static)
+    for (int64_t n = 0; n < N; ++n) {
+      const float uf = U(m, n);
+      if (uf > 0.f) {
+        const double x = uf, y = cf1[n];
+        a[0] += 1; a[1] += x; a[2] += x * x; a[3] += x * x * x; a[4] += x * x * x * x;
+        a[5] += y; a[6] += y * x; a[7] += y * x * x;
+      }
+    }
+    for (int k = 5; k < 8; ++k) a[k] *= (double)em;
+    for (int k = 0; k < 8; ++k) {
+      const double g = gsums[(size_t)m * 8 + k];
+      if (a[k] != 0 || g != 0) sum_err = std::max(sum_err, rel_diff(g, a[k]));
+    }
+    double c64[3], cg[3];
+    const int emode = solve_mode(a, c64);
+    const double* gs = gsums + (size_t)m * 8;
+    solve_mode(gs, cg);
+    mode_mis += emode != gmode;
+    if (gmode == 2) ++rdates;
+    /* R3 sums (FP64 paths, its own state) and its coefficients. */
+    double a3[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma omp parallel for reduction(+ : a3[:8]) schedule(static)
+    for (int64_t n = 0; n < N; ++n) {
+      const double x = U64(m, n);
+      if (x > 0) {
+        const double y = cf3[n] * disc[tau3[n] - m];
+        a3[0] += 1; a3[1] += x; a3[2] += x * x; a3[3] += x * x * x; a3[4] += x * x * x * x;
+        a3[5] += y; a3[6] += y * x; a3[7] += y * x * x;
+      }
+    }
+    double c3[3];
+    const int mode3 = solve_mode(a3, c3);
+    double a4[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma omp parallel for reduction(+ : a4[:8]) schedule(static)
+    for (int64_t n = 0; n < N; ++n) {
+      const double x = U(m, n);
+      if (x > 0) {
+        const double y = cf4[n] * disc[tau4[n] - m];
+        a4[0] += 1; a4[1] += x; a4[2] += x * x; a4[3] += x * x * x; a4[4] += x * x * x * x;
+        a4[5] += y; a4[6] += y * x; a4[7] += y * x * x;
+      }
+    }
+    double c4[3];
+    const int mode4 = solve_mode(a4, c4);
+
+    long long l_cflips = 0, l_flips2 = 0, l_unexpl = 0, l_itm = 0;
+    double l_fit = 0, l_fits = 0, l_cm = 0, l_fm = 0;
+#pragma omp parallel for reduction(+ : l_cflips, l_flips2, l_unexpl, l_itm) \
+    reduction(max : l_fit, l_fits, l_cm, l_fm) schedule(static)
+    for (int64_t n = 0; n < N; ++n) {
+      /* R1: the kernel's decision, replayed in FP32. */
+      const float uf = U(m, n);
+      bool d1 = false;
+      float ex1 = 0.f;
+      if (gmode != 0 && uf > 0.f) {
+        float cont;
+        ex1 = uf * Ef;
+        if (gmode == 1) {
+          cont = cf1[n] * em;
+        } else {
+          cont = fmaf(fmaf(c2, uf, c1), uf, c0);
+          if (ref_exercise) ex1 = fmaxf(fmaf(Ef, uf, nKf), 0.f);
+        }
+        d1 = ex1 > cont;
+      }
+      if (gmode == 2 && uf > 0.f) {
+        ++l_itm;
+        const double x = uf;
+        const double fg = (double)c0 + (double)c1 * x + (double)c2 * x * x;
+        l_fit = std::max(l_fit, fabs(fg - (c64[0] + c64[1] * x + c64[2] * x * x)) / E);
+        l_fits = std::max(l_fits, fabs(fg - (cg[0] + cg[1] * x + cg[2] * x * x)) / E);
+        /* The decision the FP64 coefficients would take on the same state. */
+        const double ex = ref_exercise ? std::max(E * x - pf * E, 0.0) : E * x;
+        const double f64 = ex - (c64[0] + c64[1] * x + c64[2] * x * x);
+        if ((f64 > 0) != d1) {
+          ++l_cflips;
+          l_cm = std::max(l_cm, fabs(f64) / E);
+        }
+      }
+      /* R2: FP64 path value, the GPU's coefficients. */
+      const double u2 = U64(m, n);
+      bool d2 = false;
+      if (gmode != 0 && u2 > 0) {
+        double cont, ex = E * u2;
+        if (gmode == 1) {
+          cont = cf2[n] * disc[tau2[n] - m];
+        } else {
+          cont = (double)c0 + (double)c1 * u2 + (double)c2 * u2 * u2;
+          if (ref_exercise) ex = std::max(E * u2 - pf * E, 0.0);
+        }
+        d2 = ex > cont;
+      }
+      if (d2 != d1) {
+        ++l_flips2;
+        bool explained = (u2 > 0) != (uf > 0.f);  /* in-the-money status itself */
+        if (!explained && gmode == 2) {
+          auto f = [&](double v) {
+            const double ex = ref_exercise ? std::max(E * v - pf * E, 0.0) : E * v;
+            return ex - ((double)c0 + (double)c1 * v + (double)c2 * v * v);
+          };
+          const double fu = f(uf), f2 = f(u2);
+          const double x = uf;
+          const double eps = ldexp(1.0, -21) * (fabs(E * x) + E + fabs((double)c0) +
+                                                fabs((double)c1 * x) + fabs((double)c2 * x * x));
+          explained = ((fu > 0) != (f2 > 0)) || fabs(fu) <= eps;
+          l_fm = std::max(l_fm, fabs(f2) / E);
+        } else if (!explained && gmode == 1) {
+          /* Depends on the path's own cash flow, which an earlier flip moved. */
+          explained = tau1[n] != tau2[n];
+        }
+        if (!explained) ++l_unexpl;
+      }
+      /* Apply the three decisions. */
+      if (d1) {
+        cf1[n] = ex1 * dm;
+        tau1[n] = m;
+      }
+      if (d2) {
+        cf2[n] = (ref_exercise && gmode == 2) ? std::max(E * u2 - pf * E, 0.0) : E * u2;
+        tau2[n] = m;
+      }
+      const double u4 = uf;
+      if (mode4 != 0 && u4 > 0) {
+        double cont, ex = E * u4;
+        if (mode4 == 1) {
+          cont = cf4[n] * disc[tau4[n] - m];
+        } else {
+          cont = c4[0] + c4[1] * u4 + c4[2] * u4 * u4;
+          if (ref_exercise) ex = std::max(E * u4 - pf * E, 0.0);
+        }
+        if (ex > cont) {
+          cf4[n] = ex;
+          tau4[n] = m;
+        }
+      }
+      const double u3 = u2;
+      if (mode3 != 0 && u3 > 0) {
+        double cont, ex = E * u3;
+        if (mode3 == 1) {
+          cont = cf3[n] * disc[tau3[n] - m];
+        } else {
+          cont = c3[0] + c3[1] * u3 + c3[2] * u3 * u3;
+          if (ref_exercise) ex = std::max(E * u3 - pf * E, 0.0);
+        }
+        if (ex > cont) {
+          cf3[n] = ex;
+          tau3[n] = m;
+        }
+      }
+    }
+    cflips += l_cflips;
+    flips2 += l_flips2;
+    unexpl += l_unexpl;
+    itm_dates += l_itm;
+    fit_err = std::max(fit_err, l_fit);
+    fit_err_solve = std::max(fit_err_solve, l_fits);
+    cmargin = std::max(cmargin, l_cm);
+    fmargin = std::max(fmargin, l_fm);
+  }
+  long long tmis1 = 0, tmis2 = 0, tmis3 = 0, tmis4 = 0, tmis34 = 0;
+  for (int64_t n = 0; n < N; ++n) {
+    tmis1 += tau1[n] != (int)gtau[n];
+    tmis2 += tau2[n] != (int)gtau[n];
+    tmis3 += tau3[n] != (int)gtau[n];
+    tmis4 += tau4[n] != (int)gtau[n];
+    tmis34 += tau4[n] != tau3[n];
+  }
+  /* Moments over antithetic pair means (the kernel's estimator). */
+  auto cvd = [&](int t, double Stau, double cfd, double SM) {
+    if (ref_exercise) return disc[M] * std::max(pf * (SM - E), 0.0);
+    if (t == M) return cfd;
+    return disc[t] * bs_rem(Stau, E, r, sigma, (M - t) * dtd, pf);
+  };
+  double y1 = 0, g1 = 0, y2 = 0, y3 = 0, g3 = 0, yv = 0, y4 = 0;
+  for (int64_t p = 0; p < H; ++p) {
+    double a1 = 0, b1 = 0, a2 = 0, a3 = 0, b3 = 0, av = 0, a4 = 0;
+    for (int64_t n : {p, p + H}) {
+      /* R1: the GPU's FP32 state valued in FP64. */
+      const double c = cf1[n];
+      a1 += c;
+      const double Stau = E + pf * (c * (double)edtf[tau1[n]]);
+      b1 += cvd(tau1[n], Stau, c, E * (1.0 + pf * (double)U(M, n)));
+      a2 += cf2[n] * disc[tau2[n]];
+      a3 += cf3[n] * disc[tau3[n]];
+      a4 += cf4[n] * disc[tau4[n]];
+      b3 += cvd(tau3[n], S[(size_t)tau3[n] * N + n], cf3[n] * disc[tau3[n]], S[(size_t)M * N + n]);
+      /* The GPU's exercise dates valued on FP64 paths. */
+      const int t = gtau[n];
+      const double u = U64(t, n);
+      double cfv;
+      if (t == M) cfv = E * std::max(u, 0.0);
+      else if (ref_exercise && (int)gcoef[(size_t)t * 4] == 2) cfv = std::max(E * u - pf * E, 0.0);
+      else cfv = E * u;
+      av += cfv * disc[t];
+    }
+    y1 += 0.5 * a1; g1 += 0.5 * b1; y2 += 0.5 * a2; y3 += 0.5 * a3; g3 += 0.5 * b3; yv += 0.5 * av;
+    y4 += 0.5 * a4;
+  }
+  rep[0] = (double)tmis1;
+  rep[1] = (double)mode_mis;
+  rep[2] = sum_err;
+  rep[3] = fit_err;
+  rep[4] = fit_err_solve;
+  rep[5] = (double)cflips;
+  rep[6] = cmargin;
+  rep[7] = rel_diff(gmom[0], y1);
+  rep[8] = rel_diff(gmom[2], g1);
+  rep[10] = (double)flips2;
+  rep[11] = (double)unexpl;
+  rep[12] = (double)tmis2;
+  rep[13] = rel_diff(y2, gmom[0]);
+  rep[14] = rel_diff(gmom[0], yv);
+  rep[15] = (double)tmis3;
+  rep[16] = rel_diff(y3, gmom[0]);
+  rep[17] = rel_diff(g3, gmom[2]);
+  rep[18] = fmargin;
+  rep[19] = (double)rdates;
+  rep[20] = (double)itm_dates;
+  rep[21] = (double)tmis4;
+  rep[22] = rel_diff(y4, gmom[0]);
+  rep[23] = (double)tmis34;
+  rep[24] = rel_diff(y3, y4);
 }

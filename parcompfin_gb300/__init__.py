@@ -15,6 +15,7 @@ from .api import (  # noqa: F401
     serve_trace,
     request,
     mc_amer,
+    mc_amer_audit,
     mc_amer_result,
     mc_asia,
     mc_asia_result,

@@ -133,6 +133,10 @@ SIGNATURES = {
                            C.POINTER(McResult)]),
     "pcf_mc_amer": (_I, [_P, _D, _D, _D, _D, _D, _LL, _I, _I, _I, _ULL, _I,
                          C.POINTER(McResult)]),
+    "pcf_mc_amer_audit": (_I, [_P, _D, _D, _D, _D, _D, _LL, _I, _I, _I, _ULL,
+                               C.POINTER(McResult), C.POINTER(C.c_float), _PD,
+                               C.POINTER(C.c_ushort), C.POINTER(C.c_float)]),
+    "pcf_ctx_set_test_barrier": (_I, [_P, C.c_uint, C.c_uint]),
     "pcf_mc_eur_noalloc": (_I, [_D, _D, _D, _D, _D, _LL, _I, _ULL, _P, _P]),
     "pcf_binom_embar": (_I, [_P, _D, _D, _D, _D, _D, _I, _I, _I, _PD]),
     "pcf_binom_embar_batch": (_I, [_P, _I, C.POINTER(BinomContract), _I, _PD]),

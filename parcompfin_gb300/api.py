@@ -74,6 +74,13 @@ class Context:
         """Cap each device buffer the context allocates (0: no cap)."""
         _lib.check(_lib.load().pcf_ctx_set_memory_limit(self._h, int(nbytes)))
 
+    def set_test_barrier(self, extra_arrivals: int, poll_limit: int = 1) -> None:
+        """Test hook: make the cooperative group barriers of mc_amer and the
+        lattice pricers unable to complete (extra_arrivals > 0) so that they
+        give up after poll_limit polls; 0 restores normal operation."""
+        _lib.check(_lib.load().pcf_ctx_set_test_barrier(self._h, int(extra_arrivals),
+                                                         int(poll_limit)))
+
     def close(self) -> None:
         if self._h:
             _lib.load().pcf_ctx_destroy(self._h)
@@ -154,6 +161,34 @@ def mc_amer(S0, E, r, sigma, T, N, M, payoff_fun, *, ref_exercise=False, seed=0,
 
 
 BINOM_MODES = {"reference": 0, "accurate": 1}
+
+
+def mc_amer_audit(S0, E, r, sigma, T, N, M, payoff_fun, *, ref_exercise=False, seed=0,
+                  want_paths=True, ctx=None):
+    """mc_amer with the audit record of the sweep (pcf_mc_amer_audit).
+
+    Returns (result, coef[M][4], sums[M][8], tau[N], u[M][N] or None) as
+    numpy arrays; see include/pcf.h for their meaning. A status other than
+    PCF_OK or PCF_ESINGULAR raises; on PCF_ESINGULAR the record is returned
+    with result = None."""
+    import numpy as np
+    lib = _lib.load()
+    out = _lib.McResult()
+    N, M = int(N), int(M)
+    coef = np.zeros((M, 4), np.float32)
+    sums = np.zeros((M, 8), np.float64)
+    tau = np.zeros(N, np.uint16)
+    u = np.zeros((M, N), np.float32) if want_paths else None
+    fp = C.POINTER(C.c_float)
+    st = lib.pcf_mc_amer_audit(
+        _h(ctx), S0, E, r, sigma, T, N, M, payoff_code(payoff_fun), int(bool(ref_exercise)),
+        int(seed), C.byref(out), coef.ctypes.data_as(fp),
+        sums.ctypes.data_as(C.POINTER(C.c_double)), tau.ctypes.data_as(C.POINTER(C.c_ushort)),
+        u.ctypes.data_as(fp) if u is not None else None)
+    if st == _lib.PCF_ESINGULAR:
+        return None, coef, sums, tau, u
+    _lib.check(st)
+    return out, coef, sums, tau, u
 
 
 def binom_embar(S0, E, r, sigma, T, N, payoff_fun, *, mode="reference", ctx=None) -> float:

@@ -52,6 +52,7 @@ struct LatticeParams {
   unsigned* barrier;
   int* err;
   unsigned wait_limit;
+  unsigned barrier_extra;  // test hook: arrivals the barrier expects beyond the grid
   double* out;
 };
 
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(kLatBlock) lattice_kernel(LatticeParams P, int
   // same value as payoff()).
   for (int i = b * kLatBlock + threadIdx.x; i <= P.N; i += G * kLatBlock)
     P.A[i] = lat_payoff(P, P.N, i);
-  if (!group_barrier(P.barrier, (unsigned)G, P.err, P.wait_limit)) return;
+  if (!group_barrier(P.barrier, (unsigned)G + P.barrier_extra, P.err, P.wait_limit)) return;
   double* src = P.A;
   double* dst = P.B;
   int top = P.N;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kLatBlock) lattice_kernel(LatticeParams P, int
       cur = advance(P, cur, nxt, cnt0, top, k, a);
       for (int t = threadIdx.x; t < e - a; t += kLatBlock) dst[a + t] = cur[t];
     }
-    if (!group_barrier(P.barrier, (unsigned)G, P.err, P.wait_limit)) return;
+    if (!group_barrier(P.barrier, (unsigned)G + P.barrier_extra, P.err, P.wait_limit)) return;
     double* x = src;
     src = dst;
     dst = x;
@@ -199,6 +200,10 @@ extern "C" int pcf_binom_vanilla(pcf_ctx* ctx, double S0, double E, double r, do
   P.barrier = (unsigned*)(dv + o_cnt);
   P.err = (int*)(dv + o_cnt + 64);
   P.wait_limit = 1u << 22;
+  if (c->test_barrier_extra) {  // test hook: a barrier that cannot complete
+    P.barrier_extra = c->test_barrier_extra;
+    P.wait_limit = c->test_poll_limit;
+  }
   P.out = (double*)(dv + o_out);
   int cap = seg_cap;
   void* args[] = {&P, &cap};

@@ -93,6 +93,8 @@ struct LsmParams {
   uint32_t seed_lo, seed_hi, stream;
   unsigned wait_limit;       // group-barrier polls before giving up
   unsigned copy_wait_limit;  // mbarrier polls before giving up
+  unsigned barrier_extra;    // test hook: arrivals the cooperative group barrier expects
+                             // beyond the grid (it can then never complete); 0 otherwise
   float* paths;           // M rows of 2*Hp floats
   const float* dtab;      // exp(-r dt k), k = 0..M, then exp(+r dt k), k = 0..M
   double* partial;        // 2 x nblocks x kRegSums (cooperative)
@@ -105,6 +107,12 @@ struct LsmParams {
   double* out;            // kMoments sums
   float* gcf;             // streaming sweep: 2*Hp discounted cash flows (device memory)
   unsigned short* gtau;   // streaming sweep: 2*Hp exercise dates
+  // Audit record (pcf_mc_amer_audit; NULL otherwise), written by block 0 /
+  // every block for its own paths: per date d, {mode, c0, c1, c2} and the
+  // eight regression sums as the solve saw them; per path its exercise date.
+  float* dbg_coef;        // M x 4
+  double* dbg_sums;       // M x kRegSums
+  unsigned short* dbg_tau;  // N: plus half [0, H), minus half [H, 2H)
 };
 
 // Four consecutive floats of shared memory (16-byte aligned).
@@ -349,7 +357,8 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
     }
     __syncwarp();
     int ok = 1;
-    if (lane == 0) ok = group_arrive_wait(P.barrier, (unsigned)G, P.err, P.wait_limit);
+    if (lane == 0)
+      ok = group_arrive_wait(P.barrier, (unsigned)G + P.barrier_extra, P.err, P.wait_limit);
     ok = __shfl_sync(0xffffffffu, ok, 0);
     if (!ok && lane == 0) X.fail = 1;
 #pragma unroll 4
@@ -361,6 +370,7 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
   g = df_add(g, shfl_xor_df(g, 8));
   g = df_add(g, shfl_xor_df(g, 16));  // lanes 0..7: the contract's sum q = lane
   if (q >= 5) g = df_mul(g, DF{growth, 0.f});  // y sums: cash flows grown to date d
+  if (P.dbg_sums && b == 0 && lane < kRegSums) P.dbg_sums[(size_t)d * kRegSums + lane] = df_value(g);
   // include/common.h:98-141 solves the normal equations by the adjugate over
   // the determinant, then a mat-vec product. The normal matrix of the basis
   // {1, u, u^2} is the symmetric Hankel matrix [[a0,a1,a2],[a1,a2,a3],
@@ -421,6 +431,13 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
     X.coef[0] = c0;
     X.coef[1] = c1;
     X.coef[2] = c2;
+    if (P.dbg_coef && b == 0) {
+      float* o = P.dbg_coef + (size_t)d * 4;
+      o[0] = (float)mode;
+      o[1] = c0;
+      o[2] = c1;
+      o[3] = c2;
+    }
   }
 }
 
@@ -676,6 +693,11 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
         if ((pend >> k) & 1u) mbar_wait(&S.bar[k], (ph >> k) & 1u, P.copy_wait_limit);
     return;
   }
+  if (P.dbg_tau)
+    for (int i = threadIdx.x; i < nb; i += BS) {
+      P.dbg_tau[p0 + i] = (unsigned short)S.tau[i];
+      P.dbg_tau[P.H + p0 + i] = (unsigned short)S.tau[PB + i];
+    }
 
   // ---- discounted cash flows and the control variate, per antithetic pair ----
   // Moments are taken over pair means: the two paths of a pair share their
@@ -869,6 +891,11 @@ __global__ void __launch_bounds__(kLsmBlock, 1) lsm_stream_kernel(LsmParams P) {
   }
   __syncthreads();
   if (failed) return;
+  if (P.dbg_tau)
+    for (long long i = threadIdx.x; i < nb; i += BS) {
+      P.dbg_tau[p0 + i] = P.gtau[p0 + i];
+      P.dbg_tau[P.H + p0 + i] = P.gtau[Hp + p0 + i];
+    }
 
   // ---- final moments over pair means (as lsm_body) ----
   const float* last = P.paths + (size_t)(M - 1) * stride;
@@ -1494,9 +1521,19 @@ void lsm_batch_destroy(LsmBatch* B) {
 
 using namespace pcf;
 
-extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
-                           long long N, int M, int payoff_fun, int ref_exercise,
-                           unsigned long long seed, int use_cv, pcf_mc_result* out) {
+namespace {
+
+// Optional audit record of one pcf_mc_amer call (host buffers; any may be NULL).
+struct AmerAudit {
+  float* coef;            // M x 4: per date d (index d), {mode, c0, c1, c2}
+  double* sums;           // M x 8: the regression sums the solve saw at date d
+  unsigned short* tau;    // N: exercise date per path (plus half, then minus half)
+  float* u;               // M x N: the path matrix, row m-1 = date m
+};
+
+int amer_run(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T, long long N,
+             int M, int payoff_fun, int ref_exercise, unsigned long long seed, int use_cv,
+             pcf_mc_result* out, const AmerAudit* au) {
   if (!out) return set_error(PCF_EINVAL, "out is NULL");
   int st = check_lsm_request(S0, E, r, sigma, T, N, M, payoff_fun);
   if (st) return st;
@@ -1521,7 +1558,8 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
     if (st) return st;
     if ((long long)occ * c->sm_count < G)
       return set_error(PCF_EINVAL, "LSM grid of %d blocks cannot be co-resident", G);
-    hybrid_shape(Lm, N / 2, M, G, smem, hcl, Gh, PBh);
+    // The barrier test hook runs on the plain cooperative grid only.
+    if (!c->test_barrier_extra) hybrid_shape(Lm, N / 2, M, G, smem, hcl, Gh, PBh);
   }
   const int Gmax = std::max(G, Gh);
 
@@ -1529,6 +1567,10 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   lsm_fill(P, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, 0);
   P.pairs_per_block = PB;
   P.nblocks = G;
+  if (c->test_barrier_extra) {
+    P.barrier_extra = c->test_barrier_extra;
+    P.wait_limit = c->test_poll_limit;
+  }
   // Resident path matrix: M rows x 2*Hp floats (the streaming sweep adds
   // 2*Hp cash flows and 2*Hp exercise dates).
   const size_t matrix_bytes = a256(sizeof(float) * (size_t)M * 2 * (size_t)P.Hp);
@@ -1544,13 +1586,16 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
     if (st) return st;
     c->paths_cap = paths_bytes;
   }
-  // Scratch: dtab | partial | fpartial | counters | out.
+  // Scratch: dtab | partial | fpartial | counters | out [| audit coef | sums | tau].
   const size_t o_dt = 0;
   const size_t o_part = a256(o_dt + dtab_bytes(M));
   const size_t o_fpart = a256(o_part + sizeof(double) * 2 * Gmax * kRegSums);
   const size_t o_cnt = a256(o_fpart + sizeof(double) * Gmax * kMoments);
   const size_t o_out = a256(o_cnt + sizeof(unsigned) * 4);
-  const size_t total = a256(o_out + sizeof(double) * kMoments);
+  const size_t o_acoef = a256(o_out + sizeof(double) * kMoments);
+  const size_t o_asums = a256(o_acoef + (au ? sizeof(float) * 4 * (size_t)M : 0));
+  const size_t o_atau = a256(o_asums + (au ? sizeof(double) * kRegSums * (size_t)M : 0));
+  const size_t total = a256(o_atau + (au ? sizeof(unsigned short) * (size_t)N : 0));
   st = ctx_ensure(c, total, total);
   if (st) return st;
   char* d = (char*)c->d_buf;
@@ -1560,6 +1605,8 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
                                    c->stream), "H2D dtab");
   if (!st) st = cuda_status(cudaMemsetAsync(d + o_cnt, 0, sizeof(unsigned) * 4, c->stream),
                             "memset counters");
+  if (!st && au)  // dates without a regression (date 0, skipped dates) read as mode 0
+    st = cuda_status(cudaMemsetAsync(d + o_acoef, 0, total - o_acoef, c->stream), "memset audit");
   if (st) return st;
   P.paths = (float*)c->d_paths;
   P.dtab = (const float*)(d + o_dt);
@@ -1571,6 +1618,11 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   P.err = (int*)(cnt + 2);
   P.singular = (int*)(cnt + 3);
   P.out = (double*)(d + o_out);
+  if (au) {
+    P.dbg_coef = (float*)(d + o_acoef);
+    P.dbg_sums = (double*)(d + o_asums);
+    P.dbg_tau = (unsigned short*)(d + o_atau);
+  }
   if (streaming) {
     P.gcf = (float*)((char*)c->d_paths + matrix_bytes);
     P.gtau = (unsigned short*)((char*)c->d_paths + matrix_bytes + a256(8 * (size_t)P.Hp));
@@ -1584,17 +1636,52 @@ extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double s
   }
   if (st) return st;
   c->launches += 1;
-  st = cuda_status(cudaMemcpyAsync(h + o_cnt, d + o_cnt, o_out - o_cnt + sizeof(double) * kMoments,
-                                   cudaMemcpyDeviceToHost, c->stream),
+  st = cuda_status(cudaMemcpyAsync(h + o_cnt, d + o_cnt, total - o_cnt, cudaMemcpyDeviceToHost,
+                                   c->stream),
                    "D2H lsm");
+  if (!st && au && au->u) {
+    // Row m-1 (date m): plus half [0, H) then minus half [Hp, Hp + H) of each
+    // 2*Hp-float row, into M rows of N floats.
+    const size_t pitch = sizeof(float) * 2 * (size_t)P.Hp, w = sizeof(float) * (size_t)P.H;
+    st = cuda_status(cudaMemcpy2DAsync(au->u, sizeof(float) * (size_t)N, c->d_paths, pitch, w,
+                                       (size_t)M, cudaMemcpyDeviceToHost, c->stream),
+                     "D2H audit paths (plus half)");
+    if (!st)
+      st = cuda_status(cudaMemcpy2DAsync(au->u + P.H, sizeof(float) * (size_t)N,
+                                         (const float*)c->d_paths + P.Hp, pitch, w, (size_t)M,
+                                         cudaMemcpyDeviceToHost, c->stream),
+                       "D2H audit paths (minus half)");
+  }
   if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "lsm kernel");
   if (st) return st;
+  if (au) {
+    if (au->coef) memcpy(au->coef, h + o_acoef, sizeof(float) * 4 * (size_t)M);
+    if (au->sums) memcpy(au->sums, h + o_asums, sizeof(double) * kRegSums * (size_t)M);
+    if (au->tau) memcpy(au->tau, h + o_atau, sizeof(unsigned short) * (size_t)N);
+  }
   const int* flags = (const int*)(h + o_cnt);
   if (flags[2] == 4) return set_error(PCF_ECUDA, "LSM cluster launch ran without its cluster shape");
   if (flags[2]) return set_error(PCF_ETIMEOUT, "LSM device wait gave up (code %d)", flags[2]);
   if (flags[3])
-    return set_error(PCF_ESINGULAR, "Detereminant is not > 0 at %d exercise date(s)", flags[3]);
+    return set_error(PCF_ESINGULAR, "Determinant is not > 0 at %d exercise date(s)", flags[3]);
   const double* s = (const double*)(h + o_out);
   fill_amer_result(s, N, S0, E, r, sigma, T, payoff_fun, use_cv != 0, out);
   return PCF_OK;
+}
+
+}  // namespace
+
+extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
+                           long long N, int M, int payoff_fun, int ref_exercise,
+                           unsigned long long seed, int use_cv, pcf_mc_result* out) {
+  return amer_run(ctx, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, use_cv, out,
+                  nullptr);
+}
+
+extern "C" int pcf_mc_amer_audit(pcf_ctx* ctx, double S0, double E, double r, double sigma,
+                                 double T, long long N, int M, int payoff_fun, int ref_exercise,
+                                 unsigned long long seed, pcf_mc_result* out, float* coef,
+                                 double* sums, unsigned short* tau, float* u) {
+  const AmerAudit au{coef, sums, tau, u};
+  return amer_run(ctx, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, 1, out, &au);
 }

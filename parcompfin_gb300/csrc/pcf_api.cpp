@@ -395,6 +395,17 @@ int pcf_ctx_set_memory_limit(pcf_ctx* c, unsigned long long bytes) {
   return PCF_OK;
 }
 
+int pcf_ctx_set_test_barrier(pcf_ctx* ctx, unsigned extra_arrivals, unsigned poll_limit) {
+  int st;
+  pcf_ctx* c = resolve_ctx(ctx, &st);
+  if (!c) return st;
+  if (extra_arrivals && poll_limit < 1)
+    return set_error(PCF_EINVAL, "poll_limit must be >= 1 with extra arrivals");
+  c->test_barrier_extra = extra_arrivals;
+  c->test_poll_limit = extra_arrivals ? poll_limit : 0;
+  return PCF_OK;
+}
+
 int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T, long long N,
                int payoff_fun, unsigned long long seed, int use_cv, pcf_mc_result* out) {
   if (!out) return set_error(PCF_EINVAL, "out is NULL");

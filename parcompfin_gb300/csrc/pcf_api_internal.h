@@ -32,6 +32,11 @@ struct pcf_ctx {
   void* serve = nullptr;
   // Upper bound on device bytes this context may hold (0 = unlimited).
   size_t budget_bytes = 0;
+  // Test hook (pcf_ctx_set_test_barrier): the cooperative group barriers of
+  // pcf_mc_amer and pcf_binom_vanilla expect this many arrivals beyond their
+  // grid, so they cannot complete, and give up after test_poll_limit polls.
+  unsigned test_barrier_extra = 0;
+  unsigned test_poll_limit = 0;
   long long launches = 0;
 };
 

@@ -1,8 +1,9 @@
 """Generate the golden fixtures that pin the oracle.
 
-Run from the repository root where the reference is present:
+Run from the repository root, on a machine where the reference sources are
+present, with their location as the argument:
 
-    sh oracle/build_ref.sh /root/reference     # compiles oracle/_ref/*.so
+    sh oracle/build_ref.sh REFERENCE_ROOT      # compiles oracle/_ref/*.so
     python tests/golden/gen_golden.py
 
 Writes
@@ -76,10 +77,13 @@ def ref_outputs() -> list[dict]:
             raise SystemExit(f"oracle/_ref/ref_{name}.so missing: run oracle/build_ref.sh")
         S0, E, r, sigma, T, N, M, pf = args
         seed = kw.get("seed", 0)
-        v = lib(S0, E, r, sigma, T, N, M, pf, 0, seed)
-        cases.append({"fn": name, "S0": S0, "E": E, "r": r, "sigma": sigma, "T": T, "N": N,
-                      "M": M, "payoff_fun": pf, "seed": seed, "value": v.hex(),
-                      "value_repr": repr(v)})
+        threads = kw.get("threads", 0)
+        v = lib(S0, E, r, sigma, T, N, M, pf, threads, seed)
+        case = {"fn": name, "S0": S0, "E": E, "r": r, "sigma": sigma, "T": T, "N": N,
+                "M": M, "payoff_fun": pf, "seed": seed, "value": v.hex(), "value_repr": repr(v)}
+        if threads:
+            case["threads"] = threads
+        cases.append(case)
 
     for seed in (1, 42, 1234):
         add("mc_eur", (100.0, 100.0, 0.05, 0.2, 1.0, 20000, 0, 1.0), seed=seed)
@@ -88,6 +92,10 @@ def ref_outputs() -> list[dict]:
         add("mc_asia", (100.0, 95.0, 0.04, 0.3, 0.5, 3000, 12, -1.0), seed=seed)
         add("mc_amer", (100.0, 100.0, 0.05, 0.3, 1.0, 2000, 50, -1.0), seed=seed)
         add("mc_amer", (100.0, 90.0, 0.05, 0.3, 1.0, 2000, 20, 1.0), seed=seed)
+        # The OpenMP build on one thread (its reductions then run in path order).
+        add("mc_amer_omp", (100.0, 100.0, 0.05, 0.3, 1.0, 2000, 50, -1.0), seed=seed, threads=1)
+        add("mc_amer_omp", (100.0, 90.0, 0.05, 0.3, 1.0, 2000, 20, 1.0), seed=seed, threads=1)
+        add("mc_amer_omp", (100.0, 100.0, 0.05, 0.3, 1.0, 1000, 3, 1.0), seed=seed, threads=1)
     for N in (2, 3, 100, 1000, 1001, 5000, 20000):
         for pf in (1.0, -1.0):
             add("binom_embar", (100.0, 110.0, 0.02, 0.75, 1.0, N, 0, pf))

@@ -69,6 +69,28 @@ def test_invalid_arguments_are_rejected_before_any_device_work(pcf_lib):
                                      C.byref(out)) == -1
 
 
+def test_non_finite_parameters_are_rejected(pcf_lib):
+    """NaN or infinite parameters are PCF_EINVAL on every entry point, before
+    any device work (the reference would price garbage)."""
+    out = _lib_result()
+    nan, inf = float("nan"), float("inf")
+    price = C.c_double()
+    for bad in ((nan, 100, .05, .3, 1.0), (100, nan, .05, .3, 1.0), (100, 100, nan, .3, 1.0),
+                (100, 100, .05, nan, 1.0), (100, 100, .05, .3, inf)):
+        assert pcf_lib.pcf_mc_amer(None, *bad, 4096, 10, -1, 0, 0, 0, C.byref(out)) == -1
+        assert pcf_lib.pcf_mc_eur(None, *bad, 4096, 1, 0, 0, C.byref(out)) == -1
+        assert pcf_lib.pcf_mc_asia(None, *bad, 4096, 12, 1, 0, 0, 0, C.byref(out)) == -1
+        assert pcf_lib.pcf_binom_embar(None, *bad, 1000, 1, 0, C.byref(price)) == -1
+        assert pcf_lib.pcf_binom_vanilla(None, *bad, 1000, 1, 1, C.byref(price)) == -1
+        assert pcf_lib.pcf_mc_amer_audit(None, *bad, 4096, 10, -1, 0, 0, C.byref(out), None,
+                                         None, None, None) == -1
+
+
+def _lib_result():
+    from parcompfin_gb300 import _lib
+    return _lib.McResult()
+
+
 def test_no_device_fails_loudly(pcf_lib):
     """Without a GPU the engine reports it and never falls back to the CPU."""
     try:

@@ -8,6 +8,7 @@ Bars:
   * mode "accurate" against exact 50-digit sums (tests/golden/binom_exact.json):
     1e-12 relative.
 """
+import ctypes as C
 import json
 import math
 import os
@@ -73,6 +74,44 @@ def test_reference_mode_large_n_vs_windowed_oracle(orc, ctx, N):
         part = orc.ref_binom_embar_window(S0, E, r, sig, T, N, float(pf), N // 2 - w, N)
         ref = math.exp(-r * T) * part
         assert rel(v, ref) < REF_TOL, (pf, v, ref)
+
+
+def test_binomial_book_stratified_sample_vs_reference(orc, ctx):
+    """The binomial book (1024 contracts from seed 7, N uneven in
+    1e3..2e5) priced in one launch, as the benchmark runs it; a stratified
+    sample of 32 contracts, one from each N-stratum of 32, against the
+    reference's sum at 1e-10. The oracle restates comb()'s exact sequential
+    chain for every pair index within 9 sqrt(N) + 400 of the binomial
+    weights' centres (N p and N p u / R, and their mirrors), which holds all
+    of the weight; the full O(N^2) sum would take ~25 CPU-hours for the book.
+    The sample's oracle sums run in parallel threads (ctypes releases the
+    interpreter lock)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import parcompfin_gb300 as pcf
+    from parcompfin_gb300 import workloads
+    book = workloads.binom_book()
+    got = pcf.binom_embar_batch(book, ctx=ctx)
+    order = sorted(range(len(book)), key=lambda i: book[i][5])
+    sample = order[16::32]
+    assert len(sample) == 32 and book[sample[0]][5] < 10_000 and book[sample[-1]][5] > 190_000
+
+    def ref(i):
+        S0, E, r, sig, T, N, pf = book[i]
+        lat = (C.c_double * 5)()
+        orc.ref_lattice(r, sig, T, N, lat)
+        p, u, R = lat[2], lat[0], lat[4]
+        centre = min(N * p, N * (1 - p), N * p * u / R, N * (1 - p * u / R))
+        lo = max(0, int(centre - 9 * math.sqrt(N) - 400))
+        return math.exp(-r * T) * orc.ref_binom_embar_window(S0, E, r, sig, T, N, float(pf), lo, N)
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        refs = list(ex.map(ref, sample))
+    worst = 0.0
+    for i, v in zip(sample, refs):
+        worst = max(worst, rel(got[i], v))
+        assert rel(got[i], v) < REF_TOL, (book[i], got[i], v)
+    print("binomial book sample: worst relative gap", worst)
 
 
 def test_reference_50000_survey_value(ctx):

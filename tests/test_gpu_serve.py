@@ -135,3 +135,38 @@ def test_price_batch_arena_grows_and_is_reused(ctx):
     assert list(a[0].sums) == list(c[0].sums) == list(b[-1].sums)
     for x, y in zip(b, ref):
         assert list(x.sums) == list(y.sums)
+
+
+def test_served_prices_agree_with_the_reference(orc, ctx):
+    """A seeded mixed trace of 300 requests through the serving loop, each
+    served price against its reference (oracle/served_check.py): European
+    against Black-Scholes, Asian against the reference's own estimator
+    (src/mc_asia_omp.cpp) at a combined standard error, basket against the
+    FP64 restatement on independent draws, American puts against the
+    reference's lattice (src/binom_vanilla_amer.cpp) within the LSM bias and
+    against the FP64 twin on identical draws. Outside three combined standard
+    errors, 0.27 % of the checked requests are expected by chance: at most
+    two per kind, and none beyond 4.5."""
+    import json
+    import os
+
+    import parcompfin_gb300 as pcf
+    from oracle import served_check
+    reqs, arr = _trace(pcf, 300, 4000.0, 41)
+    out, st = pcf.serve_trace(reqs, arr, target_rel_se=TARGET, ctx=ctx)
+    assert st.completed == len(reqs)
+    rep = served_check.check(orc, reqs, [o.result for o in out])
+    log = os.environ.get("PCF_AUDIT_LOG")
+    if log:
+        with open(log, "a") as f:
+            f.write(json.dumps({"served_check": rep["per_kind"]}) + "\n")
+    pk = rep["per_kind"]
+    assert set(pk) == {"eur", "asia", "basket", "amer"}
+    for k in ("eur", "asia", "basket"):
+        assert pk[k]["nan"] == 0 and pk[k]["checked"] > 30, (k, pk[k])
+        assert pk[k]["outside_3se"] <= 2, (k, pk[k])
+        assert pk[k]["max_abs_z"] < 4.5, (k, pk[k])
+    for k in ("asia", "basket"):
+        assert pk[k]["cv_mean_max_rel_err"] < 1e-9, (k, pk[k])
+    assert pk["amer"]["checked"] > 30 and pk["amer"]["outside_bar"] == 0, pk["amer"]
+    assert pk["amer"]["twin_outside"] == 0, pk["amer"]

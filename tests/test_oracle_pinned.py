@@ -51,6 +51,8 @@ def _call_oracle(orc, c):
         return orc.ref_mc_asia(*a, c["N"], c["M"], pf, c["seed"])
     if fn == "mc_amer":
         return orc.ref_mc_amer(*a, c["N"], c["M"], pf, c["seed"])
+    if fn == "mc_amer_omp":
+        return orc.ref_mc_amer_omp(*a, c["N"], c["M"], pf, c["seed"], c["threads"])
     if fn == "binom_embar":
         return orc.ref_binom_embar(*a, c["N"], pf)
     if fn == "binom_vanilla_eur":
