@@ -848,7 +848,14 @@ ORC_EXPORT void twin_mc_amer(double S0, double E, double r, double sigma, double
  * 20 in-the-money path-dates of the regression dates, 21 R4 exercise dates
  * differing from the GPU's, 22 relative difference of sum y (R4 vs GPU),
  * 23 exercise dates differing between R4 and R3, 24 relative difference of
- * sum y (R3 vs R4).
+ * sum y (R3 vs R4), 25 the first date (in the backward sweep) at which R4's
+ * decisions differ from the GPU's (0: never), 26 the paths that differ
+ * there, 27 their largest |exercise - continuation| / E under R4's FP64
+ * coefficients, 28 the largest difference of the GPU's and R4's fitted
+ * continuation values at that date (/E). Up to that date the two states are
+ * identical; after it each flip moves the later regressions, which flips
+ * further paths near the boundary (the estimator is a discontinuous
+ * function of its inputs), so later differences are consequences.
  *
  * R4  the GPU's FP32 path matrix with FP64 regressions and FP64 decisions
  *     (no replay): R4 against the GPU isolates the kernel's arithmetic, R3
@@ -879,7 +886,7 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
                                    uint32_t stream, const float* gcoef, const double* gsums,
                                    const uint16_t* gtau, const float* gu, const double* gmom,
                                    double* rep) {
-  for (int k = 0; k < 25; ++k) rep[k] = 0;
+  for (int k = 0; k < 29; ++k) rep[k] = 0;
   const int64_t H = N / 2;
   const double dtd = T / M;
   /* The kernel's FP32 constants, made as the host makes them. */
@@ -935,6 +942,13 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
   for (int64_t n = 0; n < N; ++n) cf4[n] = E * std::max((double)U(M, n), 0.0);
 
   long long mode_mis = 0, cflips = 0, flips2 = 0, unexpl = 0, rdates = 0, itm_dates = 0;
+  /* R4 against the GPU: the first date (in the backward sweep) where their
+   * decisions differ, the paths that differ there and how far those lie from
+   * the boundary; before it the two states are identical. */
+  bool synced4 = true;
+  int first4 = 0;
+  long long first4_paths = 0;
+  double first4_margin = 0, first4_fitdiff = 0;
   double sum_err = 0, fit_err = 0, fit_err_solve = 0, cmargin = 0, fmargin = 0;
   for (int m = M - 1; m >= 1; --m) {
     const int gmode = (int)gcoef[(size_t)m * 4];
@@ -989,10 +1003,10 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
     double c4[3];
     const int mode4 = solve_mode(a4, c4);
 
-    long long l_cflips = 0, l_flips2 = 0, l_unexpl = 0, l_itm = 0;
-    double l_fit = 0, l_fits = 0, l_cm = 0, l_fm = 0;
-#pragma omp parallel for reduction(+ : l_cflips, l_flips2, l_unexpl, l_itm) \
-    reduction(max : l_fit, l_fits, l_cm, l_fm) schedule(static)
+    long long l_cflips = 0, l_flips2 = 0, l_unexpl = 0, l_itm = 0, l_d4 = 0;
+    double l_fit = 0, l_fits = 0, l_cm = 0, l_fm = 0, l_m4 = 0, l_fd4 = 0;
+#pragma omp parallel for reduction(+ : l_cflips, l_flips2, l_unexpl, l_itm, l_d4) \
+    reduction(max : l_fit, l_fits, l_cm, l_fm, l_m4, l_fd4) schedule(static)
     for (int64_t n = 0; n < N; ++n) {
       /* R1: the kernel's decision, replayed in FP32. */
       const float uf = U(m, n);
@@ -1066,6 +1080,7 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
         tau2[n] = m;
       }
       const double u4 = uf;
+      bool d4 = false;
       if (mode4 != 0 && u4 > 0) {
         double cont, ex = E * u4;
         if (mode4 == 1) {
@@ -1074,7 +1089,16 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
           cont = c4[0] + c4[1] * u4 + c4[2] * u4 * u4;
           if (ref_exercise) ex = std::max(E * u4 - pf * E, 0.0);
         }
-        if (ex > cont) {
+        d4 = ex > cont;
+        if (synced4 && mode4 == 2 && gmode == 2) {
+          const double fg = (double)c0 + (double)c1 * u4 + (double)c2 * u4 * u4;
+          l_fd4 = std::max(l_fd4, fabs(fg - (c4[0] + c4[1] * u4 + c4[2] * u4 * u4)) / E);
+          if (d4 != d1) {
+            ++l_d4;
+            l_m4 = std::max(l_m4, fabs(ex - cont) / E);
+          }
+        }
+        if (d4) {
           cf4[n] = ex;
           tau4[n] = m;
         }
@@ -1093,6 +1117,13 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
           tau3[n] = m;
         }
       }
+    }
+    if (synced4 && l_d4 > 0) {
+      synced4 = false;
+      first4 = m;
+      first4_paths = l_d4;
+      first4_margin = l_m4;
+      first4_fitdiff = l_fd4;
     }
     cflips += l_cflips;
     flips2 += l_flips2;
@@ -1166,4 +1197,8 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
   rep[22] = rel_diff(y4, gmom[0]);
   rep[23] = (double)tmis34;
   rep[24] = rel_diff(y3, y4);
+  rep[25] = (double)first4;
+  rep[26] = (double)first4_paths;
+  rep[27] = first4_margin;
+  rep[28] = first4_fitdiff;
 }

@@ -38,7 +38,9 @@ AUDIT_KEYS = ["r1_tau_mismatch", "r1_mode_mismatch", "sums_rel_err", "fit_err_ov
               "r2_flips", "r2_unexplained", "r2_tau_diff", "r2_price_rel",
               "gpu_vs_fp64_value_of_gpu_policy", "r3_tau_diff", "r3_price_rel", "r3_cv_rel",
               "r2_flip_margin_over_E", "regression_dates", "itm_path_dates",
-              "r4_tau_diff", "r4_price_rel", "r3_vs_r4_tau_diff", "r3_vs_r4_price_rel"]
+              "r4_tau_diff", "r4_price_rel", "r3_vs_r4_tau_diff", "r3_vs_r4_price_rel",
+              "r4_first_divergence_date", "r4_first_divergence_paths",
+              "r4_first_divergence_margin_over_E", "r4_first_divergence_fit_diff_over_E"]
 
 
 def twin(orc, S0, E, r, sig, T, N, M, pf, ref_ex, seed):
@@ -52,7 +54,7 @@ def audit(orc, ctx, S0, E, r, sig, T, N, M, pf, ref_ex, seed):
     from parcompfin_gb300.api import mc_amer_audit
     res, coef, sums, tau, u = mc_amer_audit(S0, E, r, sig, T, N, M, pf, ref_exercise=ref_ex,
                                             seed=seed, ctx=ctx)
-    rep = (C.c_double * 25)()
+    rep = (C.c_double * 29)()
     mom = (C.c_double * 5)(*res.sums)
     fp = C.POINTER(C.c_float)
     orc.twin_mc_amer_audit(S0, E, r, sig, T, N, M, pf, int(ref_ex), seed, 0,
@@ -89,6 +91,16 @@ def test_amer_policy_audit(orc, ctx, pf, N, M):
     assert a["r2_unexplained"] == 0, a
     assert a["gpu_vs_fp64_value_of_gpu_policy"] < 1e-5, a
     assert a["regression_dates"] == M - 1, a
+    # R4: FP64 regressions and decisions on the GPU's paths. Up to the first
+    # date where they differ, the two states are identical; the decisions
+    # that differ there lie within the fitted values' difference (the FP32
+    # rounding of the coefficients) plus the FP32 evaluation error of the
+    # boundary. Later differences are that flip's cascade through the later
+    # regressions, and the independent twin's differences (R3) are the same
+    # cascade: R3 against R4 (FP64 against FP32 paths) differ far less.
+    if a["r4_first_divergence_date"]:
+        assert a["r4_first_divergence_margin_over_E"] <= (
+            a["r4_first_divergence_fit_diff_over_E"] + 1e-6), a
 
 
 @pytest.mark.parametrize("pf", [-1, 1])
