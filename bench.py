@@ -110,6 +110,9 @@ class EurWorkload:
         import parcompfin_gb300 as pcf
         self.plan = pcf.Plan(self.reqs, ctx=ctx)
 
+    def tune_requests(self):
+        return self.reqs
+
     def step(self, ctx):
         self.plan.launch()
 
@@ -179,6 +182,7 @@ class AsiaWorkload:
                      for i, c in enumerate(self.cs)]
 
     setup = EurWorkload.setup
+    tune_requests = EurWorkload.tune_requests
     step = EurWorkload.step
 
     def finish(self, ctx):
@@ -250,6 +254,7 @@ class BasketWorkload:
                      for i, c in enumerate(self.cs)]
 
     setup = EurWorkload.setup
+    tune_requests = EurWorkload.tune_requests
     step = EurWorkload.step
 
     def finish(self, ctx):
@@ -462,7 +467,8 @@ class MixedWorkload:
     dominant = "lsm_cluster_kernel (American, one cluster per contract)"
     R = 1000             # requests per step
     TARGET = 5e-4        # relative standard error
-    LOADS = (1000, 10000, 50000)
+    LOADS = (1000, 10000, 50000)             # offered requests/s, 1 s of arrivals each
+    SATURATION = (100000, 200000, 400000)    # beyond the engine's burst rate
 
     def __init__(self, rank):
         import parcompfin_gb300 as pcf
@@ -568,6 +574,9 @@ class MixedWorkload:
             pilot.append((se_cv, p_cv, se_pl, disc * m))
         self._sizes(pilot)
 
+    def tune_requests(self):
+        return self.main
+
     def step(self, ctx):
         self.plan.launch()
 
@@ -657,17 +666,19 @@ class MixedWorkload:
         """Served latency at offered loads, and the plain one-contract-per-launch path."""
         import parcompfin_gb300 as pcf
         from parcompfin_gb300 import workloads
-        served = {}
-        for rate in self.LOADS:
-            n = int(min(4 * self.R, max(self.R, rate * 1.0)))
+        served, saturation = {}, {}
+        for rate in self.LOADS + self.SATURATION:
+            # At least one second of Poisson arrivals at each offered load.
+            n = int(max(self.R, rate * 1.0))
             spec = workloads.mixed_stream(n, seed=29 + rate)
             reqs = [self._req(pcf, s, 0) for s in spec]
             arr = workloads.poisson_arrivals(n, rate, seed=31 + rate)
             out, st = pcf.serve_trace(reqs, arr, target_rel_se=self.TARGET, ctx=ctx)
-            served[str(rate)] = {"offered_per_s": rate, "requests": n, "p50_ms": st.p50_ms,
-                                 "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
-                                 "contracts_per_s": st.contracts_per_s,
-                                 "paths_per_s": st.paths_per_s, "batches": st.batches}
+            rec = {"offered_per_s": rate, "requests": n, "arrivals_s": arr[-1],
+                   "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
+                   "max_ms": st.max_ms, "contracts_per_s": st.contracts_per_s,
+                   "paths_per_s": st.paths_per_s, "batches": st.batches}
+            (served if rate in self.LOADS else saturation)[str(rate)] = rec
         # Plain path: each request alone, plain estimator, at the path count the
         # plain estimator needs for the same standard error.
         k = min(60, len(self.spec))
@@ -697,7 +708,7 @@ class MixedWorkload:
                  "note": "each request alone through its single-contract entry point, plain "
                          "estimator, at the path count the plain estimator needs for the same "
                          "5e-4 relative standard error (American capped at 2^21)"}
-        return {"served": served, "plain_gpu": plain}
+        return {"served": served, "saturation": saturation, "plain_gpu": plain}
 
     def cpu_reference(self, threads, budget_s, step=0):
         """The reference's OpenMP pricers on the host cores, for the same
@@ -812,6 +823,7 @@ class AmerBatchWorkload:
                                  stream=rank * 4096 + i) for i in range(self.C)]
 
     setup = EurWorkload.setup
+    tune_requests = EurWorkload.tune_requests
     step = EurWorkload.step
     e2e = EurWorkload.e2e
 
@@ -968,6 +980,24 @@ def run_ours(args, wl_cls):
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     wl.setup(ctx)
+    tune_reqs = wl.tune_requests() if hasattr(wl, "tune_requests") else None
+    if args.no_tune or not tune_reqs:
+        tuning = {"table": ctx.tuning()["table"], "changed": [],
+                  "note": "built-in work shapes" if args.no_tune else
+                          "no launch of this workload takes its shape from the table"}
+    else:
+        # The autotuner times candidate work shapes on this workload's own
+        # batch (untimed), then the workload is set up again under the table
+        # it chose; the bench line reports that table.
+        t0 = time.perf_counter()
+        rep = ctx.autotune(requests=tune_reqs)
+        tuning = {"seconds": time.perf_counter() - t0, "mode": rep["mode"], "table": rep["table"],
+                  "changed": sorted(k for k in rep["table"]
+                                    if k != "tuned" and rep["table"][k] != rep["built_in"][k])}
+        if args.tune_report:
+            with open(args.tune_report, "w") as f:
+                json.dump(rep, f)
+        wl.setup(ctx)
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -1040,6 +1070,7 @@ def run_ours(args, wl_cls):
         "e2e": {"value": e2e_units / (e2e_med * 1e-3) if e2e_ms else None, "unit": wl.unit,
                 "h2d_bytes_per_step": io[0], "d2h_bytes_per_step": io[1], "ms_per_step": e2e_med},
         "gpu_launches": launches,
+        "tuning": tuning,
         "clocks": clk,
         "check": check,
     }
@@ -1078,6 +1109,8 @@ def main():
     ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the built-in work shapes")
+    ap.add_argument("--tune-report", default="", help="write the autotuner's full report here")
     args = ap.parse_args()
     if args.impl == "ours":
         args.warmup = max(args.warmup, 3)

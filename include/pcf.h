@@ -43,6 +43,7 @@ extern "C" {
 #define PCF_ETIMEOUT (-4)   /* a bounded device wait gave up */
 #define PCF_ECUDA (-5)      /* CUDA runtime error */
 #define PCF_ENODEV (-6)     /* no CUDA device */
+#define PCF_PENDING 1       /* not an error: a served request is not finished yet */
 
 typedef struct pcf_ctx pcf_ctx;
 
@@ -283,6 +284,41 @@ PCF_API int pcf_plan_destroy(pcf_plan* plan);
 PCF_API int pcf_price_batch(pcf_ctx* ctx, int n, const pcf_mc_request* reqs,
                             pcf_mc_result* results);
 
+/* ---- Work shapes and the autotuner ---------------------------------------
+ * Every launch takes its work shape from a per-device table: the block size
+ * of the Monte Carlo launches (128, 256 or 512 threads), the paths each
+ * thread prices in one work item (by class of N for European contracts, of
+ * M for Asian ones, of d for baskets), the 128-path tiles per work item of
+ * the tensor-core basket kernel, and the Longstaff-Schwartz cluster size and
+ * slice (by class of N). The built-in table was measured by hand on GB300.
+ * A work item's size depends only on its contract and the table, so results
+ * are the same alone and in any batch while the table is unchanged; a new
+ * table regroups the per-thread sums (differences of ~1e-8 relative).
+ * The reference's only knob is a fixed OpenMP chunk of 1000 paths
+ * (schedule(dynamic,1000), src/mc_eur_omp.cpp:24). */
+#define PCF_TUNE_MC 1    /* European, Asian and basket shapes */
+#define PCF_TUNE_LSM 2   /* Longstaff-Schwartz cluster shapes */
+#define PCF_TUNE_SAVE 4  /* write the table to the file named by PCF_TUNE_CACHE */
+
+/* Times candidate shapes per method and shape class on the context's device
+ * (plans of synthetic contracts of each class, CUDA events, best of three)
+ * and keeps a candidate where it beats the shape in force by more than 2 %.
+ * flags = 0 tunes everything. Writes a JSON report (the table, the built-in
+ * table and every trial) to report[report_len] if report is not NULL. Takes
+ * seconds. A file named by the environment variable PCF_TUNE_CACHE is read
+ * on a device's first use, if it was written for the same device model. */
+PCF_API int pcf_autotune(pcf_ctx* ctx, int flags, char* report, int report_len);
+/* pcf_autotune with every knob timed on the caller's own batch (a plan of
+ * reqs[n], e.g. a representative slice of a served stream), so the table
+ * fits that workload rather than each shape class alone. */
+PCF_API int pcf_autotune_batch(pcf_ctx* ctx, int flags, int n, const pcf_mc_request* reqs,
+                               char* report, int report_len);
+/* The table in force on the context's device, as JSON
+ * {"device": ..., "table": {...}}. */
+PCF_API int pcf_tune_report(pcf_ctx* ctx, char* report, int report_len);
+/* Restores the built-in table on the context's device. */
+PCF_API int pcf_tune_reset(pcf_ctx* ctx);
+
 /* ---- Serving ---------------------------------------------------------------
  * A continuous-batching loop. Requests arrive over time; every request whose
  * arrival time has passed is admitted into the next free batch slot. Slots
@@ -330,6 +366,33 @@ typedef struct pcf_server_stats {
 PCF_API int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg, int n,
                             const pcf_mc_request* reqs, const double* arrival_s,
                             pcf_served_result* out, pcf_server_stats* stats);
+
+/* The live server: the same continuous-batching loop on a worker thread of
+ * its own, fed by callers while it runs (pcf_serve_trace replays a trace
+ * known in advance). pcf_server_start reserves the context's serving slots
+ * (kept in the context, as for pcf_serve_trace) and starts the worker; from
+ * then until pcf_server_stop the context belongs to the server (no other call
+ * may use it). Any thread may submit, poll and wait. A request's arrival time
+ * is its submission, on the server's clock (seconds since start). Results
+ * do not depend on what else is being served: the same request alone gives
+ * the same result (the batching and the work shapes depend on the request
+ * alone). No counterpart in the reference. */
+typedef struct pcf_server pcf_server;
+PCF_API int pcf_server_start(pcf_ctx* ctx, const pcf_server_config* cfg, pcf_server** out);
+/* Queues one request; *ticket identifies it (0, 1, 2, ... in submission
+ * order). The request is copied; arrays it points to (basket_S0,
+ * basket_sigma, corr) must stay valid until its result is available. */
+PCF_API int pcf_server_submit(pcf_server* srv, const pcf_mc_request* req, long long* ticket);
+/* PCF_OK and *out filled if the request is finished (out->status holds its
+ * own error, if any), PCF_PENDING if not yet. */
+PCF_API int pcf_server_poll(pcf_server* srv, long long ticket, pcf_served_result* out);
+/* As pcf_server_poll, waiting up to timeout_s seconds (< 0: no limit). */
+PCF_API int pcf_server_wait(pcf_server* srv, long long ticket, double timeout_s,
+                            pcf_served_result* out);
+/* Finishes every submitted request, stops the worker, fills stats over all
+ * requests served and frees the server (the slots stay with the context).
+ * Returns the first batch error, if any. */
+PCF_API int pcf_server_stop(pcf_server* srv, pcf_server_stats* stats);
 
 #ifdef __cplusplus
 }

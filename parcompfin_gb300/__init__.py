@@ -7,6 +7,7 @@ the reference's.
 from .api import (  # noqa: F401
     Context,
     Plan,
+    Server,
     binom_embar,
     binom_embar_batch,
     binom_vanilla_amer,

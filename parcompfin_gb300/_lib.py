@@ -20,6 +20,7 @@ PCF_ESINGULAR = -3
 PCF_ETIMEOUT = -4
 PCF_ECUDA = -5
 PCF_ENODEV = -6
+PCF_PENDING = 1
 
 
 class PcfError(RuntimeError):
@@ -52,6 +53,7 @@ class McResult(C.Structure):
 
 
 METHOD_EUR, METHOD_ASIA, METHOD_BASKET, METHOD_AMER = 0, 1, 2, 3
+TUNE_MC, TUNE_LSM, TUNE_SAVE = 1, 2, 4
 
 
 class McRequest(C.Structure):
@@ -137,6 +139,10 @@ SIGNATURES = {
                                C.POINTER(McResult), C.POINTER(C.c_float), _PD,
                                C.POINTER(C.c_ushort), C.POINTER(C.c_float)]),
     "pcf_ctx_set_test_barrier": (_I, [_P, C.c_uint, C.c_uint]),
+    "pcf_autotune": (_I, [_P, _I, C.c_char_p, _I]),
+    "pcf_autotune_batch": (_I, [_P, _I, _I, C.POINTER(McRequest), C.c_char_p, _I]),
+    "pcf_tune_report": (_I, [_P, C.c_char_p, _I]),
+    "pcf_tune_reset": (_I, [_P]),
     "pcf_mc_eur_noalloc": (_I, [_D, _D, _D, _D, _D, _LL, _I, _ULL, _P, _P]),
     "pcf_binom_embar": (_I, [_P, _D, _D, _D, _D, _D, _I, _I, _I, _PD]),
     "pcf_binom_embar_batch": (_I, [_P, _I, C.POINTER(BinomContract), _I, _PD]),
@@ -149,6 +155,11 @@ SIGNATURES = {
     "pcf_plan_kernel_count": (_I, [_P]),
     "pcf_plan_destroy": (_I, [_P]),
     "pcf_price_batch": (_I, [_P, _I, C.POINTER(McRequest), C.POINTER(McResult)]),
+    "pcf_server_start": (_I, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "pcf_server_submit": (_I, [_P, C.POINTER(McRequest), C.POINTER(C.c_longlong)]),
+    "pcf_server_poll": (_I, [_P, C.c_longlong, C.POINTER(ServedResult)]),
+    "pcf_server_wait": (_I, [_P, C.c_longlong, _D, C.POINTER(ServedResult)]),
+    "pcf_server_stop": (_I, [_P, C.POINTER(ServerStats)]),
     "pcf_serve_trace": (_I, [_P, C.POINTER(ServerConfig), _I, C.POINTER(McRequest), _PD,
                              C.POINTER(ServedResult), C.POINTER(ServerStats)]),
 }

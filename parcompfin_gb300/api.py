@@ -81,6 +81,34 @@ class Context:
         _lib.check(_lib.load().pcf_ctx_set_test_barrier(self._h, int(extra_arrivals),
                                                          int(poll_limit)))
 
+    def autotune(self, mc: bool = True, lsm: bool = True, save: bool = False,
+                 requests=None) -> dict:
+        """Time candidate work shapes on this device and keep the fastest
+        (pcf_autotune; with `requests`, pcf_autotune_batch times every knob on
+        that batch); returns the JSON report as a dict."""
+        import json
+        flags = (_lib.TUNE_MC if mc else 0) | (_lib.TUNE_LSM if lsm else 0) | \
+            (_lib.TUNE_SAVE if save else 0)
+        buf = C.create_string_buffer(1 << 16)
+        if requests:
+            arr, keep = _pack(requests)
+            _lib.check(_lib.load().pcf_autotune_batch(self._h, flags, len(requests), arr, buf,
+                                                      len(buf)))
+        else:
+            _lib.check(_lib.load().pcf_autotune(self._h, flags, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def tuning(self) -> dict:
+        """The work-shape table in force on this device."""
+        import json
+        buf = C.create_string_buffer(4096)
+        _lib.check(_lib.load().pcf_tune_report(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def tune_reset(self) -> None:
+        """Restore the built-in work shapes on this device."""
+        _lib.check(_lib.load().pcf_tune_reset(self._h))
+
     def close(self) -> None:
         if self._h:
             _lib.load().pcf_ctx_destroy(self._h)
@@ -353,3 +381,54 @@ def mc_basket_result(S0s, sigmas, corr, r, T, E, N, payoff_fun, *, scale_by_sqrt
                                  payoff_code(payoff_fun), int(bool(scale_by_sqrt_T)),
                                  int(seed), int(bool(use_cv)), C.byref(out)))
     return out
+
+
+class Server:
+    """The live continuous-batching server (pcf_server_*): start it on a
+    context, submit requests from any thread while it runs, poll or wait for
+    each result by its ticket, stop it to drain and get the latency stats.
+    The context belongs to the server until stop()."""
+
+    def __init__(self, ctx, *, target_rel_se=5e-4, pilot_paths=1 << 14, max_paths=1 << 26,
+                 max_amer_paths=1 << 21, max_batch=2048, slots=12, hbm_fraction=0.5):
+        lib = _lib.load()
+        cfg = _lib.ServerConfig(float(target_rel_se), int(pilot_paths), int(max_paths),
+                                int(max_amer_paths), int(max_batch), int(slots),
+                                float(hbm_fraction))
+        h = C.c_void_p()
+        _lib.check(lib.pcf_server_start(_h(ctx), C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def submit(self, req) -> int:
+        arr, keep = _pack([req])
+        self._keep.append(keep)
+        t = C.c_longlong()
+        _lib.check(_lib.load().pcf_server_submit(self._h, arr, C.byref(t)))
+        return t.value
+
+    def poll(self, ticket):
+        """The ServedResult if finished, else None."""
+        out = _lib.ServedResult()
+        st = _lib.load().pcf_server_poll(self._h, int(ticket), C.byref(out))
+        if st == _lib.PCF_PENDING:
+            return None
+        _lib.check(st)
+        return out
+
+    def wait(self, ticket, timeout_s=-1.0):
+        out = _lib.ServedResult()
+        st = _lib.load().pcf_server_wait(self._h, int(ticket), float(timeout_s), C.byref(out))
+        if st == _lib.PCF_PENDING:
+            return None
+        _lib.check(st)
+        return out
+
+    def stop(self):
+        """Drain, stop and return the ServerStats."""
+        stats = _lib.ServerStats()
+        st = _lib.load().pcf_server_stop(self._h, C.byref(stats))
+        self._h = None
+        if st not in (_lib.PCF_OK, _lib.PCF_ESINGULAR):
+            _lib.check(st)
+        return stats

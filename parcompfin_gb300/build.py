@@ -34,6 +34,7 @@ SOURCES = [
     ("pcf_batch.cpp", []),
     ("pcf_server.cpp", []),
     ("pcf_math.cpp", []),
+    ("pcf_tune.cpp", []),
 ]
 
 

@@ -1205,16 +1205,39 @@ constexpr int kNumPB = 5;
 // flight, and each CTA pays the per-date exchange once for more paths.
 // (Measured: one 1024-thread CTA per SM holding the same 8192 pairs ran the
 // 64-put batch no faster and the mixed stream 4 % slower.)
-bool cluster_shape(const LsmLimits& Lm, long long H, int M, int& cl, int& k, bool& t8) {
+// `shift` (the tuning table's, by class of N) moves off that choice: +1
+// doubles the cluster and halves the slice, -1 halves the cluster and
+// doubles the slice (one CTA per SM where two no longer fit), when the
+// device allows the result; the CTAs still cover the contract.
+bool cluster_shape(const LsmLimits& Lm, long long H, int M, int shift, int& cl, int& k,
+                   bool& t8) {
   t8 = M <= 255;
   const size_t tb = t8 ? 1 : 2, stat = t8 ? Lm.stat8 : Lm.stat16;
-  for (cl = 1; cl <= Lm.cl_max; cl *= 2)
+  bool found = false;
+  for (cl = 1; cl <= Lm.cl_max && !found; cl *= 2)
     for (k = 0; k < kNumPB; ++k)
-      if ((long long)cl * kLsmPB[k] >= H && lsm_fits(Lm, kLsmPB[k], M, tb, stat, 2)) return true;
-  cl = Lm.cl_max;
-  for (k = 0; k < kNumPB; ++k)
-    if ((long long)cl * kLsmPB[k] >= H && lsm_fits(Lm, kLsmPB[k], M, tb, stat, 1)) return true;
-  return false;
+      if ((long long)cl * kLsmPB[k] >= H && lsm_fits(Lm, kLsmPB[k], M, tb, stat, 2)) {
+        found = true;
+        break;
+      }
+  if (found) {
+    cl /= 2;  // undo the loop's last doubling
+  } else {
+    cl = Lm.cl_max;
+    for (k = 0; k < kNumPB && !found; ++k)
+      if ((long long)cl * kLsmPB[k] >= H && lsm_fits(Lm, kLsmPB[k], M, tb, stat, 1)) found = true;
+    if (!found) return false;
+    --k;  // undo the loop's last increment
+  }
+  if (shift > 0 && k > 0 && 2 * cl <= Lm.cl_max && lsm_fits(Lm, kLsmPB[k - 1], M, tb, stat, 2)) {
+    cl *= 2;
+    --k;
+  } else if (shift < 0 && cl > 1 && k + 1 < kNumPB &&
+             lsm_fits(Lm, kLsmPB[k + 1], M, tb, stat, 1)) {
+    cl /= 2;
+    ++k;
+  }
+  return true;
 }
 
 }  // namespace
@@ -1284,13 +1307,15 @@ int group_of(int cl, int k, bool t8) {
 int lsm_layout(pcf_ctx* c, const std::vector<LsmRequest>& reqs, LsmLayout& L) {
   const LsmLimits& Lm = lsm_limits(c);
   if (Lm.status) return Lm.status;
+  const TuneTable tt = tune_table(c->device);
   const size_t n = reqs.size();
   L.group.assign(n, -1);
   L.members.assign(kLsmGroups, {});
   for (size_t i = 0; i < n; ++i) {
     int cl, k;
     bool t8;
-    if (cluster_shape(Lm, reqs[i].N / 2, reqs[i].M, cl, k, t8)) {
+    if (cluster_shape(Lm, reqs[i].N / 2, reqs[i].M, tt.lsm_shift[lsm_class(reqs[i].N)], cl, k,
+                      t8)) {
       L.group[i] = group_of(cl, k, t8);
       L.members[L.group[i]].push_back((int)i);
     }

@@ -16,7 +16,9 @@
 // two thirds of them Philox and Box-Muller, against 3 SFU operations), so the
 // control-variate sums are compiled in only when a launch asks for them (CV
 // template flag). Baskets of 17 to 64 assets run mc_basket_tc_kernel, which
-// multiplies the normals by the correlation factor on the tensor cores.
+// multiplies the normals by the correlation factor on the tensor cores, from
+// the basket size the tuning table routes there (17 to 32 assets can also
+// run the CUDA-core kernel; above 32 they always take the tensor cores).
 //
 // Reference loops these kernels replace:
 //   European  src/mc_eur.cpp:22-26,  src/mc_eur_omp.cpp:24-27
@@ -58,19 +60,19 @@ __device__ __forceinline__ float payoff(const McContract& C, float S) {
 // European: item j covers path quads [j*U, (j+1)*U), U = units_per_item.
 // Quad q's four paths take the four normals of Philox block (x=q, y=0).
 // S_T = 2^(log2 S0 + a2 + b2 z); y = payoff(S_T), g = S_T.
-template <bool CV>
+template <bool CV, int BS>
 __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>& mo) {
   const long long nq = (C.N + 3) >> 2;
   const long long nfull = C.N >> 2;  // quads whose four paths are all < N
   const long long q0 = (long long)j * C.units_per_item + threadIdx.x;
-  const int qpt = C.units_per_item / kBlock;
+  const int qpt = C.units_per_item / BS;
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_EUR};
   const float a2 = C.a2 + C.l2S0;
   for (int k0 = 0; k0 < qpt; k0 += 4) {
     float cy = 0.f, cyy = 0.f, cg = 0.f, cgg = 0.f, cyg = 0.f;
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
-      const long long q = q0 + (long long)(k0 + kk) * kBlock;
+      const long long q = q0 + (long long)(k0 + kk) * BS;
       if (k0 + kk < qpt && q < nq) {
         const float4 z = normals4(draw_words(key, (uint64_t)(C.x0 + q), 0u));
         float s[4] = {ex2_approx(fmaf(C.b2, z.x, a2)), ex2_approx(fmaf(C.b2, z.y, a2)),
@@ -97,8 +99,8 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
   }
 }
 
-// Asian: item j covers paths [j*U, (j+1)*U), U = units_per_item, U/256 per
-// thread (path j*U + k*256 + thread); increment m uses lane m%4 of Philox block
+// Asian: item j covers paths [j*U, (j+1)*U), U = units_per_item, U/BS per
+// thread (path j*U + k*BS + thread); increment m uses lane m%4 of Philox block
 // (x=path, y=m/4). log2(S/S0) is accumulated, S = S0 * 2^L.
 // mode 0 (reference, src/mc_asia.cpp:31-35): I += S_m (c1 + c2 z_m) with S_m
 //   the level before the step; A = I/M.
@@ -148,14 +150,14 @@ __device__ __forceinline__ void asia_path(const McContract& C, const RngKey& key
   mo.add(Y, G);
 }
 
-template <bool CV>
+template <bool CV, int BS>
 __device__ __forceinline__ void asia_item(const McContract& C, int j, Moments<CV>& mo) {
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_ASIA};
   const float w = 1.f / (float)C.M;
-  const int ppt = C.units_per_item / kBlock;
+  const int ppt = C.units_per_item / BS;
 #pragma unroll 1
   for (int k = 0; k < ppt; ++k) {
-    const long long n = (long long)j * C.units_per_item + (long long)k * kBlock + threadIdx.x;
+    const long long n = (long long)j * C.units_per_item + (long long)k * BS + threadIdx.x;
     if (n >= C.N) break;
     if (C.mode == 0) asia_path<0, CV>(C, key, n, w, mo);
     else asia_path<1, CV>(C, key, n, w, mo);
@@ -223,17 +225,17 @@ __device__ __forceinline__ void basket_path(const McContract& C, const float* fb
   mo.add(Y, G);
 }
 
-// Basket item j covers paths [j*U, (j+1)*U), U = units_per_item: U/256 paths
-// per thread (path j*U + k*256 + thread), one after the other (the loop is
+// Basket item j covers paths [j*U, (j+1)*U), U = units_per_item: U/BS paths
+// per thread (path j*U + k*BS + thread), one after the other (the loop is
 // not unrolled, so a path's unrolled factor product keeps its registers).
-template <int DMAX, bool CV>
+template <int DMAX, bool CV, int BS>
 __device__ __forceinline__ void basket_item(const McContract& C, int j, const float* fb,
                                             Moments<CV>& mo) {
   const long long n0 = (long long)j * C.units_per_item + threadIdx.x;
-  const int ppt = C.units_per_item / kBlock;
+  const int ppt = C.units_per_item / BS;
 #pragma unroll 1
   for (int k = 0; k < ppt; ++k) {
-    const long long n = n0 + (long long)k * kBlock;
+    const long long n = n0 + (long long)k * BS;
     if (n >= C.N) break;
     basket_path<DMAX, CV>(C, fb, n, mo);
   }
@@ -249,13 +251,23 @@ __device__ __forceinline__ int find_contract(const int* start, int n, int item) 
   return lo;
 }
 
-// Persistent launch: blocks take work items from a queue in increasing
-// order. The next ticket is taken while the current item runs, and the item's
-// contract is found in one round: the contract is the block's previous one or
-// one of the next 255, so each thread tests one candidate (a binary search
-// covers longer jumps).
-template <int METHOD, int DMAX, bool CV>
-__global__ void __launch_bounds__(kBlock, DMAX >= 64 ? 2 : (METHOD == MC_EUR ? 5 : 4))
+// Threads resident per SM that a block size's launch bound keeps (the
+// register budget per thread is the same for every block size).
+template <int METHOD, int DMAX, int BS>
+constexpr int mc_min_blocks() {
+  return (DMAX >= 64 ? 2 : (METHOD == MC_EUR ? 5 : 4)) * 256 / BS > 0
+             ? (DMAX >= 64 ? 2 : (METHOD == MC_EUR ? 5 : 4)) * 256 / BS
+             : 1;
+}
+
+// Persistent launch: blocks of BS threads take work items from a queue in
+// increasing order. The next ticket is taken while the current item runs, and
+// the item's contract is found in one round: the contract is the block's
+// previous one or one of the next BS - 1, so each thread tests one candidate
+// (a binary search covers longer jumps). A work item is one block's worth of
+// paths: units_per_item = BS x (paths or quads per thread).
+template <int METHOD, int DMAX, bool CV, int BS>
+__global__ void __launch_bounds__(BS, (mc_min_blocks<METHOD, DMAX, BS>()))
 mc_kernel(McLaunch L) {
   __shared__ DF sh[32 * kMoments];
   __shared__ int s_item[2];
@@ -295,15 +307,15 @@ mc_kernel(McLaunch L) {
     const int j = item - base;
     Moments<CV> mo;
     if (METHOD == MC_EUR) {
-      eur_item<CV>(C, j, mo);
+      eur_item<CV, BS>(C, j, mo);
     } else if (METHOD == MC_ASIA) {
-      asia_item<CV>(C, j, mo);
+      asia_item<CV, BS>(C, j, mo);
     } else {
       if (loaded != c) {  // the previous item's readers are past the final barrier
         // Host layout [l0 (d) | v (d) | L (d x d)] -> padded [l0 | v | L rows of DMAX].
         const int d = C.M;
         const float* src = L.basket_data + C.basket_off;
-        for (int i = threadIdx.x; i < (2 + DMAX) * DMAX; i += kBlock) {
+        for (int i = threadIdx.x; i < (2 + DMAX) * DMAX; i += BS) {
           const int row = i / DMAX, col = i % DMAX;
           float v = 0.f;
           if (row < 2) {
@@ -316,7 +328,7 @@ mc_kernel(McLaunch L) {
         __syncthreads();
         loaded = c;
       }
-      basket_item<DMAX, CV>(C, j, s_fb, mo);
+      basket_item<DMAX, CV, BS>(C, j, s_fb, mo);
     }
     DF v[kMoments] = {df_of(mo.y), df_of(mo.yy), df_of(mo.g), df_of(mo.gg), df_of(mo.yg)};
     DF tot[kMoments];
@@ -622,40 +634,63 @@ int tc_max_active(void) {
 
 constexpr size_t basket_smem(int dmax) { return (size_t)(2 + dmax) * dmax * sizeof(float); }
 
-template <int METHOD, int DMAX, bool CV>
+template <int METHOD, int DMAX, bool CV, int BS>
 cudaError_t launch_one(const McLaunch& L, int grid, cudaStream_t s) {
   const size_t smem = METHOD == MC_BASKET ? basket_smem(DMAX) : 0;
-  mc_kernel<METHOD, DMAX, CV><<<grid, kBlock, smem, s>>>(L);
+  mc_kernel<METHOD, DMAX, CV, BS><<<grid, BS, smem, s>>>(L);
   return cudaGetLastError();
 }
 
-template <int METHOD, int DMAX>
+template <int METHOD, int DMAX, int BS>
 cudaError_t launch_cv(const McLaunch& L, int grid, cudaStream_t s) {
-  return L.cv ? launch_one<METHOD, DMAX, true>(L, grid, s)
-              : launch_one<METHOD, DMAX, false>(L, grid, s);
+  return L.cv ? launch_one<METHOD, DMAX, true, BS>(L, grid, s)
+              : launch_one<METHOD, DMAX, false, BS>(L, grid, s);
 }
 
 template <int METHOD, int DMAX>
-int max_active(void) {
+cudaError_t launch_bs(const McLaunch& L, int grid, int block, cudaStream_t s) {
+  switch (block) {
+    case 128: return launch_cv<METHOD, DMAX, 128>(L, grid, s);
+    case 256: return launch_cv<METHOD, DMAX, 256>(L, grid, s);
+    case 512: return launch_cv<METHOD, DMAX, 512>(L, grid, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int METHOD, int DMAX, int BS>
+int max_active_bs(void) {
   int n = 0;
   const size_t smem = METHOD == MC_BASKET ? basket_smem(DMAX) : 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mc_kernel<METHOD, DMAX, true>, kBlock,
-                                                    smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mc_kernel<METHOD, DMAX, true, BS>, BS,
+                                                    smem) != cudaSuccess) {
+    cudaGetLastError();
     return 1;
+  }
   return n > 0 ? n : 1;
+}
+
+template <int METHOD, int DMAX>
+int max_active(int block) {
+  switch (block) {
+    case 128: return max_active_bs<METHOD, DMAX, 128>();
+    case 512: return max_active_bs<METHOD, DMAX, 512>();
+    default: return max_active_bs<METHOD, DMAX, 256>();
+  }
 }
 
 }  // namespace
 
-cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, cudaStream_t s) {
+cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, int block, bool tensor,
+                      cudaStream_t s) {
   if (grid <= 0) return cudaSuccess;
   switch (m) {
-    case MC_EUR: return launch_cv<MC_EUR, 4>(L, grid, s);
-    case MC_ASIA: return launch_cv<MC_ASIA, 4>(L, grid, s);
+    case MC_EUR: return launch_bs<MC_EUR, 4>(L, grid, block, s);
+    case MC_ASIA: return launch_bs<MC_ASIA, 4>(L, grid, block, s);
     case MC_BASKET:
-      if (max_d <= 4) return launch_cv<MC_BASKET, 4>(L, grid, s);
-      if (max_d <= 8) return launch_cv<MC_BASKET, 8>(L, grid, s);
-      if (max_d <= 16) return launch_cv<MC_BASKET, 16>(L, grid, s);
+      if (max_d <= 4) return launch_bs<MC_BASKET, 4>(L, grid, block, s);
+      if (max_d <= 8) return launch_bs<MC_BASKET, 8>(L, grid, block, s);
+      if (max_d <= 16) return launch_bs<MC_BASKET, 16>(L, grid, block, s);
+      if (max_d <= 32 && !tensor) return launch_bs<MC_BASKET, 32>(L, grid, block, s);
       if (max_d <= 32) return L.cv ? launch_tc<32, true>(L, grid, s) : launch_tc<32, false>(L, grid, s);
       if (max_d <= 64) return L.cv ? launch_tc<64, true>(L, grid, s) : launch_tc<64, false>(L, grid, s);
       return cudaErrorInvalidValue;
@@ -663,14 +698,15 @@ cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, cudaSt
   return cudaErrorInvalidValue;
 }
 
-int mc_max_active_blocks(McMethod m, int max_d) {
+int mc_max_active_blocks(McMethod m, int max_d, int block, bool tensor) {
   switch (m) {
-    case MC_EUR: return max_active<MC_EUR, 4>();
-    case MC_ASIA: return max_active<MC_ASIA, 4>();
+    case MC_EUR: return max_active<MC_EUR, 4>(block);
+    case MC_ASIA: return max_active<MC_ASIA, 4>(block);
     case MC_BASKET:
-      if (max_d <= 4) return max_active<MC_BASKET, 4>();
-      if (max_d <= 8) return max_active<MC_BASKET, 8>();
-      if (max_d <= 16) return max_active<MC_BASKET, 16>();
+      if (max_d <= 4) return max_active<MC_BASKET, 4>(block);
+      if (max_d <= 8) return max_active<MC_BASKET, 8>(block);
+      if (max_d <= 16) return max_active<MC_BASKET, 16>(block);
+      if (max_d <= 32 && !tensor) return max_active<MC_BASKET, 32>(block);
       if (max_d <= 32) return tc_max_active<32>();
       return tc_max_active<64>();
   }
@@ -716,7 +752,7 @@ __global__ void __launch_bounds__(kBlock) mc_eur_noalloc_kernel(McContract C,
   float2* partial = (float2*)(scratch + kNoAllocTicketBytes);
   const int j = blockIdx.x;
   Moments<true> mo;
-  eur_item<true>(C, j, mo);
+  eur_item<true, kBlock>(C, j, mo);
   DF v[kMoments] = {df_of(mo.y), df_of(mo.yy), df_of(mo.g), df_of(mo.gg), df_of(mo.yg)};
   DF tot[kMoments];
   block_sum_df<kMoments>(v, sh, tot);
@@ -766,7 +802,9 @@ extern "C" int pcf_mc_eur_noalloc(double S0, double E, double r, double sigma, d
   unsigned char* scratch = nullptr;
   st = noalloc_setup(&scratch, dev);
   if (st) return st;
-  const McContract C = make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0);
+  // The built-in work shape (256-thread items of at most 64 quads per
+  // thread), whatever a tuner chose: the scratch size above is derived from it.
+  const McContract C = make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0, TuneTable{});
   if (C.items > kNoAllocMaxItems)
     return set_error(PCF_EINVAL, "N = %lld needs %d work items; the fixed scratch holds %d", N,
                      C.items, kNoAllocMaxItems);

@@ -90,7 +90,8 @@ pcf_ctx* resolve_ctx(pcf_ctx* ctx, int* status) {
 // Runs one batch of MC contracts of one method and returns the moment sums
 // (C * kMoments doubles). Contracts must have units_per_item and items set.
 int run_mc(pcf_ctx* c, McMethod m, std::vector<McContract>& cs, const std::vector<float>& fb,
-           int max_d, bool persistent, bool cv, std::vector<double>& sums) {
+           int max_d, int block, bool tensor, bool persistent, bool cv,
+           std::vector<double>& sums) {
   const int C = (int)cs.size();
   std::vector<int> start((size_t)C + 1, 0);
   for (int i = 0; i < C; ++i) {
@@ -135,8 +136,9 @@ int run_mc(pcf_ctx* c, McMethod m, std::vector<McContract>& cs, const std::vecto
   L.persistent = persistent ? 1 : 0;
   L.cv = cv ? 1 : 0;
   int grid = items;
-  if (persistent) grid = std::min(items, c->sm_count * mc_max_active_blocks(m, max_d));
-  st = cuda_status(launch_mc(m, L, grid, max_d, c->stream), "mc kernel launch");
+  if (persistent)
+    grid = std::min(items, c->sm_count * mc_max_active_blocks(m, max_d, block, tensor));
+  st = cuda_status(launch_mc(m, L, grid, max_d, block, tensor, c->stream), "mc kernel launch");
   if (st) return st;
   c->launches += 1;
   st = cuda_status(cudaMemcpyAsync(h, L.out, sizeof(double) * kMoments * C,
@@ -188,30 +190,8 @@ static void split_seed(unsigned long long seed, McContract& k) {
   k.seed_hi = (uint32_t)(seed >> 32);
 }
 
-// Work-item sizes depend on the contract alone, so a contract's sums are the
-// same whatever batch, launch or device prices it. An item carries enough
-// path work per thread to amortise its fixed cost (a queue ticket, the
-// contract lookup, a block reduction of five double-float sums and one
-// partial store).
-int eur_quads_per_thread(long long N) {
-  const long long nq = (N + 3) / 4;
-  long long per = nq / ((long long)kBlock * 32);  // about 32 items per contract
-  per = std::max(1LL, std::min(64LL, per));
-  return (int)(per >= 4 ? per & ~3LL : per);  // chunks of 4 quads per Kahan flush
-}
-
-// Asian: at least ~512 monitoring steps per thread per item (256: 2 % slower
-// on the 256-contract book).
-int asia_paths_per_thread(int M) { return std::max(1, std::min(32, (512 + M - 1) / M)); }
-
-// Basket: 16 / 8 / 8 paths per thread for up to 4 / 8 / 16 assets (an item
-// pays one block reduction; items of one path per thread spent more than
-// half of a 16-asset path's instructions on it); wider baskets run the
-// tensor-core kernel, whose items are 8 tiles of 128 paths.
-int basket_paths_per_thread(int d) { return d <= 4 ? 16 : d <= 8 ? 8 : d <= 16 ? 8 : 4; }
-
 McContract make_eur(double S0, double E, double r, double sigma, double T, long long N, int pf,
-                    unsigned long long seed, uint32_t stream) {
+                    unsigned long long seed, uint32_t stream, const TuneTable& t) {
   McContract k;
   memset(&k, 0, sizeof k);
   const double log2e = 1.4426950408889634;
@@ -223,7 +203,7 @@ McContract make_eur(double S0, double E, double r, double sigma, double T, long 
   k.l2S0 = (float)(log(S0) * log2e);
   k.nK = (float)(-pf * E);
   k.N = N;
-  k.units_per_item = kBlock * eur_quads_per_thread(N);
+  k.units_per_item = t.eur_block * eur_quads_per_thread(N, t);
   k.items = (int)(((N + 3) / 4 + k.units_per_item - 1) / k.units_per_item);
   split_seed(seed, k);
   k.stream = stream;
@@ -231,7 +211,8 @@ McContract make_eur(double S0, double E, double r, double sigma, double T, long 
 }
 
 McContract make_asia(double S0, double E, double r, double sigma, double T, long long N, int M,
-                     int pf, int mode, unsigned long long seed, uint32_t stream) {
+                     int pf, int mode, unsigned long long seed, uint32_t stream,
+                     const TuneTable& t) {
   McContract k;
   memset(&k, 0, sizeof k);
   const double log2e = 1.4426950408889634;
@@ -248,7 +229,7 @@ McContract make_asia(double S0, double E, double r, double sigma, double T, long
   k.M = M;
   k.mode = mode;
   k.N = N;
-  k.units_per_item = kBlock * asia_paths_per_thread(M);
+  k.units_per_item = t.asia_block * asia_paths_per_thread(M, t);
   k.items = (int)((N + k.units_per_item - 1) / k.units_per_item);
   split_seed(seed, k);
   k.stream = stream;
@@ -265,7 +246,8 @@ double asia_cv_mean(double S0, double E, double r, double sigma, double T, int M
 // Builds the basket contract and appends its factor block to fb.
 int make_basket(int d, const double* S0, const double* sig, const double* corr, double r,
                 double T, double E, long long N, int pf, double ts, unsigned long long seed,
-                uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g) {
+                uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g,
+                const TuneTable& t) {
   if (d < 1 || d > 64) return set_error(PCF_EINVAL, "assets must be in [1, 64]");
   for (int a = 0; a < d; ++a) {
     if (!(S0[a] > 0) || !(sig[a] >= 0) || !std::isfinite(S0[a]) || !std::isfinite(sig[a]))
@@ -286,7 +268,7 @@ int make_basket(int d, const double* S0, const double* sig, const double* corr, 
   k.mode = tri ? 0 : 1;
   k.nK = (float)(-pf * E);
   k.N = N;
-  k.units_per_item = kBlock * basket_paths_per_thread(d);
+  k.units_per_item = basket_units_per_item(d, t);
   k.items = (int)((N + k.units_per_item - 1) / k.units_per_item);
   split_seed(seed, k);
   k.stream = stream;
@@ -414,9 +396,10 @@ int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double
   if (N > (1LL << 46)) return set_error(PCF_EINVAL, "N must be <= 2^46");
   pcf_ctx* c = resolve_ctx(ctx, &st);
   if (!c) return st;
-  std::vector<McContract> cs{make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0)};
+  const TuneTable tt = tune_table(c->device);
+  std::vector<McContract> cs{make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0, tt)};
   std::vector<double> sums;
-  st = run_mc(c, MC_EUR, cs, {}, 0, false, use_cv != 0, sums);
+  st = run_mc(c, MC_EUR, cs, {}, 0, tt.eur_block, false, false, use_cv != 0, sums);
   if (st) return st;
   fill_result(sums.data(), N, S0 * exp(r * T), exp(-r * T), use_cv != 0, out);
   return PCF_OK;
@@ -433,9 +416,10 @@ int pcf_mc_asia(pcf_ctx* ctx, double S0, double E, double r, double sigma, doubl
   if (N > (1LL << 38)) return set_error(PCF_EINVAL, "N must be <= 2^38");
   pcf_ctx* c = resolve_ctx(ctx, &st);
   if (!c) return st;
-  std::vector<McContract> cs{make_asia(S0, E, r, sigma, T, N, M, payoff_fun, mode, seed, 0)};
+  const TuneTable tt = tune_table(c->device);
+  std::vector<McContract> cs{make_asia(S0, E, r, sigma, T, N, M, payoff_fun, mode, seed, 0, tt)};
   std::vector<double> sums;
-  st = run_mc(c, MC_ASIA, cs, {}, 0, false, use_cv != 0, sums);
+  st = run_mc(c, MC_ASIA, cs, {}, 0, tt.asia_block, false, false, use_cv != 0, sums);
   if (st) return st;
   fill_result(sums.data(), N, asia_cv_mean(S0, E, r, sigma, T, M, payoff_fun, mode),
               exp(-r * T), use_cv != 0, out);
@@ -454,12 +438,14 @@ int pcf_mc_basket(pcf_ctx* ctx, int d, const double* S0, const double* sigma, co
   std::vector<float> fb;
   McContract k;
   double mu_g = 0;
+  const TuneTable tt = tune_table(c->device);
   st = make_basket(d, S0, sigma, corr, r, T, E, N, payoff_fun, scale_by_sqrt_T ? sqrt(T) : 1.0,
-                   seed, 0, fb, k, mu_g);
+                   seed, 0, fb, k, mu_g, tt);
   if (st) return st;
   std::vector<McContract> cs{k};
   std::vector<double> sums;
-  st = run_mc(c, MC_BASKET, cs, fb, d, false, use_cv != 0, sums);
+  st = run_mc(c, MC_BASKET, cs, fb, d, mc_block(PCF_METHOD_BASKET, d, tt), basket_tensor(d, tt),
+              false, use_cv != 0, sums);
   if (st) return st;
   fill_result(sums.data(), N, mu_g, exp(-r * T), use_cv != 0, out);
   return PCF_OK;

@@ -10,6 +10,7 @@
 
 #include "../../include/pcf.h"
 #include "pcf_internal.h"
+#include "pcf_tune.h"
 
 struct pcf_ctx {
   int device = 0;
@@ -52,15 +53,18 @@ int check_common(double S0, double E, double r, double sigma, double T, long lon
 void fill_result(const double* s, long long n, double mu_g, double disc, bool use_cv,
                  pcf_mc_result* out);
 
+// Contract builders; the work-item sizes come from the tuning table.
 McContract make_eur(double S0, double E, double r, double sigma, double T, long long N, int pf,
-                    unsigned long long seed, uint32_t stream);
+                    unsigned long long seed, uint32_t stream, const TuneTable& t);
 McContract make_asia(double S0, double E, double r, double sigma, double T, long long N, int M,
-                     int pf, int mode, unsigned long long seed, uint32_t stream);
+                     int pf, int mode, unsigned long long seed, uint32_t stream,
+                     const TuneTable& t);
 double asia_cv_mean(double S0, double E, double r, double sigma, double T, int M, int pf,
                     int mode);
 int make_basket(int d, const double* S0, const double* sig, const double* corr, double r,
                 double T, double E, long long N, int pf, double ts, unsigned long long seed,
-                uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g);
+                uint32_t stream, std::vector<float>& fb, McContract& k, double& mu_g,
+                const TuneTable& t);
 
 // The reference's beta-parametrised lattice (binom.cu).
 void lattice(double r, double sigma, double T, int N, double& u, double& d, double& p,

@@ -29,7 +29,7 @@ namespace {
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int build_request(const pcf_mc_request& q, int idx, McContract& k, std::vector<float>& fb,
-                  double& mu_g, double& disc) {
+                  double& mu_g, double& disc, const TuneTable& t) {
   int st = check_common(q.method == PCF_METHOD_BASKET && q.basket_S0 ? 1.0 : q.S0, q.E, q.r,
                         q.sigma, q.T, q.N, q.payoff_fun);
   if (st) return set_error(st, "request %d: %s", idx, pcf_last_error());
@@ -37,14 +37,14 @@ int build_request(const pcf_mc_request& q, int idx, McContract& k, std::vector<f
   switch (q.method) {
     case PCF_METHOD_EUR:
       if (q.N > (1LL << 46)) return set_error(PCF_EINVAL, "request %d: N too large", idx);
-      k = make_eur(q.S0, q.E, q.r, q.sigma, q.T, q.N, q.payoff_fun, q.seed, q.stream);
+      k = make_eur(q.S0, q.E, q.r, q.sigma, q.T, q.N, q.payoff_fun, q.seed, q.stream, t);
       mu_g = q.S0 * exp(q.r * q.T);
       return PCF_OK;
     case PCF_METHOD_ASIA:
       if (q.M < 1 || q.M > (1 << 20) || (q.mode != 0 && q.mode != 1) || q.N > (1LL << 38))
         return set_error(PCF_EINVAL, "request %d: bad Asian M/mode/N", idx);
       k = make_asia(q.S0, q.E, q.r, q.sigma, q.T, q.N, q.M, q.payoff_fun, q.mode, q.seed,
-                    q.stream);
+                    q.stream, t);
       mu_g = asia_cv_mean(q.S0, q.E, q.r, q.sigma, q.T, q.M, q.payoff_fun, q.mode);
       return PCF_OK;
     case PCF_METHOD_BASKET: {
@@ -65,7 +65,7 @@ int build_request(const pcf_mc_request& q, int idx, McContract& k, std::vector<f
         for (int a = 0; a < d; ++a) cor[(size_t)a * d + a] = 1.0;
       }
       st = make_basket(d, s0.data(), sg.data(), cor.data(), q.r, q.T, q.E, q.N, q.payoff_fun,
-                       q.scale_by_sqrt_T ? sqrt(q.T) : 1.0, q.seed, q.stream, fb, k, mu_g);
+                       q.scale_by_sqrt_T ? sqrt(q.T) : 1.0, q.seed, q.stream, fb, k, mu_g, t);
       if (st) return set_error(st, "request %d: %s", idx, pcf_last_error());
       return PCF_OK;
     }
@@ -76,8 +76,13 @@ int build_request(const pcf_mc_request& q, int idx, McContract& k, std::vector<f
 }
 
 // Basket launches are split by width class so narrow baskets do not run in
-// the register-heavy instantiation of wide ones.
-int basket_class(int d) { return d <= 4 ? 0 : d <= 8 ? 1 : d <= 16 ? 2 : d <= 32 ? 3 : 4; }
+// the register-heavy instantiation of wide ones; 17 to 32 assets go to the
+// tensor-core group or, below the tuning table's threshold, to a CUDA-core
+// group of their own.
+int basket_group(int d, const TuneTable& t) {
+  if (d > 16 && d <= 32 && !basket_tensor(d, t)) return 5;
+  return basket_class_of(d);
+}
 
 }  // namespace
 
@@ -95,8 +100,10 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
   p->disc.resize(n);
   p->use_cv.resize(n);
   p->out_slot.resize(n);
-  // Groups: European, Asian, then one per basket width class.
-  const int kGroups = 7;
+  // Groups: European, Asian, then one per basket width class. Work shapes
+  // come from the device's tuning table.
+  const TuneTable tt = tune_table(c->device);
+  const int kGroups = 8;
   std::vector<Group> g(kGroups);
   g[0].method = MC_EUR;
   g[1].method = MC_ASIA;
@@ -121,9 +128,9 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
       delete p;
       return set_error(PCF_EINVAL, "request %d: method %d not supported in a batch", i, m);
     }
-    const int gi = m == PCF_METHOD_BASKET ? 2 + basket_class(reqs[i].assets) : m;
+    const int gi = m == PCF_METHOD_BASKET ? 2 + basket_group(reqs[i].assets, tt) : m;
     McContract k;
-    st = build_request(reqs[i], i, k, g[gi].fb, p->mu_g[i], p->disc[i]);
+    st = build_request(reqs[i], i, k, g[gi].fb, p->mu_g[i], p->disc[i], tt);
     if (st) {
       delete p;
       return st;
@@ -135,7 +142,11 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
       }
       k.x0 = m == PCF_METHOD_EUR ? path0[i] / 4 : path0[i];
     }
-    if (m == PCF_METHOD_BASKET) g[gi].max_d = std::max(g[gi].max_d, reqs[i].assets);
+    if (m == PCF_METHOD_BASKET) {
+      g[gi].max_d = std::max(g[gi].max_d, reqs[i].assets);
+      g[gi].tensor = basket_tensor(reqs[i].assets, tt);
+    }
+    g[gi].block = mc_block(m, m == PCF_METHOD_BASKET ? reqs[i].assets : 0, tt);
     p->npaths[i] = reqs[i].N;
     p->use_cv[i] = reqs[i].use_cv != 0;
     g[gi].cs.push_back(k);
@@ -246,7 +257,8 @@ int plan_build(pcf_ctx* c, int n, const pcf_mc_request* reqs, cudaStream_t s, Ex
     L.persistent = 1;
     L.cv = 0;
     for (int i = 0; i < C; ++i) L.cv |= p->use_cv[gr.req[i]];
-    gr.grid = std::min(L.total_items, c->sm_count * mc_max_active_blocks(gr.method, gr.max_d));
+    gr.grid = std::min(L.total_items, c->sm_count * mc_max_active_blocks(gr.method, gr.max_d,
+                                                                          gr.block, gr.tensor));
     row += C;
   }
   if (upload) {
@@ -323,7 +335,8 @@ int plan_enqueue(pcf_plan* p) {
     if (st) return st;
   }
   for (Group& gr : p->groups) {
-    int st = cuda_status(launch_mc(gr.method, gr.L, gr.grid, gr.max_d, p->stream),
+    int st = cuda_status(launch_mc(gr.method, gr.L, gr.grid, gr.max_d, gr.block, gr.tensor,
+                                   p->stream),
                          "batch kernel launch");
     if (st) return st;
     c->launches += 1;

@@ -11,7 +11,7 @@ namespace pcf {
 // {sum y, sum y^2, sum g, sum g^2, sum y*g}, y the undiscounted payoff and g
 // the kernel's control variate.
 constexpr int kMoments = 5;
-constexpr int kBlock = 256;  // threads per work item of the MC kernels
+constexpr int kBlock = 256;  // threads per work item of the MC kernels (the default)
 
 // One Monte Carlo contract as the kernels see it. Per-path arithmetic is
 // FP32; the drift/vol terms are pre-multiplied by log2(e) on the host so each
@@ -54,8 +54,12 @@ struct McLaunch {
 enum McMethod { MC_EUR = 0, MC_ASIA = 1, MC_BASKET = 2 };
 
 // Launchers (mc_kernels.cu). `grid` = blocks to launch (items, or the
-// persistent block count).
-cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, cudaStream_t s);
-int mc_max_active_blocks(McMethod m, int max_d);
+// persistent block count); `block` = threads per block (128, 256 or 512; the
+// contracts' units_per_item are multiples of it). `tensor`: baskets of 17 to
+// 32 assets run the tensor-core kernel (block fixed at 128 threads) instead
+// of the CUDA-core one; above 32 assets the tensor-core kernel always runs.
+cudaError_t launch_mc(McMethod m, const McLaunch& L, int grid, int max_d, int block, bool tensor,
+                      cudaStream_t s);
+int mc_max_active_blocks(McMethod m, int max_d, int block, bool tensor);
 
 }  // namespace pcf

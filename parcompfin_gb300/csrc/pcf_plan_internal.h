@@ -9,6 +9,8 @@ namespace pcf {
 struct Group {  // one persistent Monte Carlo launch
   McMethod method;
   int max_d = 0;
+  int block = kBlock;         // threads per block (the tuning table's, for this group)
+  bool tensor = false;        // baskets: the tensor-core kernel
   std::vector<int> req;       // request index of each contract (queue order)
   std::vector<McContract> cs;
   std::vector<float> fb;

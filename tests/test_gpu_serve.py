@@ -170,3 +170,60 @@ def test_served_prices_agree_with_the_reference(orc, ctx):
         assert pk[k]["cv_mean_max_rel_err"] < 1e-9, (k, pk[k])
     assert pk["amer"]["checked"] > 30 and pk["amer"]["outside_bar"] == 0, pk["amer"]
     assert pk["amer"]["twin_outside"] == 0, pk["amer"]
+
+
+def test_live_server_admits_while_running_and_matches_alone(ctx):
+    """The live server (pcf_server_*): two host threads submit a mixed stream
+    while earlier batches run. Every request completes near its target; some
+    are admitted while others are still on the device (more than one batch
+    in flight); and each result is the one that request gets alone at the
+    same path count (exactly, or to 1e-8 where its main run continued its
+    pilot, as in the trace replay)."""
+    import threading
+    import time
+
+    import parcompfin_gb300 as pcf
+    reqs, _ = _trace(pcf, 200, 4000.0, 5)
+    srv = pcf.Server(ctx, target_rel_se=TARGET)
+    tickets = {}
+    lock = threading.Lock()
+
+    def feed(lo, hi, gap):
+        for i in range(lo, hi):
+            t = srv.submit(reqs[i])
+            with lock:
+                tickets[i] = t
+            time.sleep(gap)
+
+    th = [threading.Thread(target=feed, args=(0, 100, 4e-4)),
+          threading.Thread(target=feed, args=(100, 200, 3e-4))]
+    for t in th:
+        t.start()
+    first = srv.poll(tickets.get(0, 0)) if tickets else None  # may well be pending
+    for t in th:
+        t.join()
+    out = {i: srv.wait(tickets[i], 120.0) for i in range(200)}
+    stats = srv.stop()
+    assert first is None or first.status == 0
+    assert all(o is not None and o.status == 0 for o in out.values())
+    assert stats.completed == 200 and stats.batches >= 2
+    assert stats.p50_ms <= stats.p99_ms <= stats.max_ms
+    ad = sorted((o.admit_s, o.done_s) for o in out.values())
+    overlap = sum(1 for k in range(1, len(ad)) if ad[k][0] < max(d for _, d in ad[:k]) and
+                  ad[k][0] > ad[k - 1][0])
+    assert overlap > 0
+    for i, o in out.items():
+        assert o.done_s >= o.admit_s >= o.arrival_s - 1e-9
+        if not (reqs[i]["method"] == 3 and o.result.n_paths >= (1 << 21)):
+            assert o.result.std_error / abs(o.result.price) < 1.35 * TARGET
+    continued = 0
+    for i in range(0, 200, 5):
+        q = dict(reqs[i], N=out[i].result.n_paths)
+        alone = pcf.price_batch([q], ctx=ctx)[0]
+        if q["method"] == 3 or q["N"] <= PILOT:
+            assert list(alone.sums) == list(out[i].result.sums), q
+        else:
+            continued += 1
+            for a, b in zip(alone.sums, out[i].result.sums):
+                assert abs(a - b) <= 1e-8 * max(abs(a), abs(b)), (q, a, b)
+    assert continued > 0
