@@ -390,11 +390,11 @@ class ServeLoop {
       s.pilot_n.clear();
       std::vector<pcf_mc_request> q;
       const double ta = now();
+      // The batch also stops where its American path matrices would no
+      // longer fit the slot (a pilot runs in one piece).
+      size_t used = 1 << 20;
       while (!pending_.empty() && s.ids.size() < share) {
         const int id = pending_.front();
-        pending_.pop_front();
-        s.ids.push_back(id);
-        rec_[id].admit_s = ta;
         pcf_mc_request r = rq_[id];
         if (cfg_.target_rel_se > 0) {
           // A multiple of 4: the main run of a European, Asian or basket
@@ -405,6 +405,12 @@ class ServeLoop {
                     ? round_up(std::max(cfg_.pilot_paths, kAmerFloor), 2)
                     : round_up(cfg_.pilot_paths, 4);
         }
+        const size_t need = cfg_.target_rel_se > 0 ? main_bytes(r) : 4096;
+        if (!s.ids.empty() && used + need > s.d_cap) break;
+        used += need;
+        pending_.pop_front();
+        s.ids.push_back(id);
+        rec_[id].admit_s = ta;
         s.pilot_n.push_back(r.N);
         q.push_back(r);
       }

@@ -243,7 +243,7 @@ using namespace pcf;
 namespace {
 
 // Times a plan of `reqs` on the context's stream: one untimed launch, then
-// the best of three, each bracketed by CUDA events (ms).
+// the best of five, each bracketed by CUDA events (ms).
 int time_plan(pcf_ctx* c, const std::vector<pcf_mc_request>& reqs, double* ms) {
   pcf_plan* p = nullptr;
   int st = pcf_plan_create(c, (int)reqs.size(), reqs.data(), &p);
@@ -253,7 +253,7 @@ int time_plan(pcf_ctx* c, const std::vector<pcf_mc_request>& reqs, double* ms) {
   if (!st) st = cuda_status(cudaEventCreate(&e1), "tune event");
   if (!st) st = pcf_plan_launch(p);
   double best = 1e30;
-  for (int k = 0; k < 3 && !st; ++k) {
+  for (int k = 0; k < 5 && !st; ++k) {
     st = cuda_status(cudaEventRecord(e0, c->stream), "tune event record");
     if (!st) st = pcf_plan_launch(p);
     if (!st) st = cuda_status(cudaEventRecord(e1, c->stream), "tune event record");
@@ -303,15 +303,24 @@ struct Tuner {
   // Times the batch (the caller's, if one was given) under each candidate
   // edit of the table and keeps the fastest, provided it beats the table in
   // force by more than 2 %.
+  // `applies`: whether the caller's batch holds work this knob shapes (a
+  // knob that shapes none of it is left alone rather than tuned on noise).
+  // The shape in force is timed first and again last, and a candidate must
+  // beat the better of the two.
   template <typename Edit>
   void choose(const char* what, const std::vector<int>& cands, int current,
-              const std::vector<pcf_mc_request>& synthetic, Edit edit) {
+              const std::vector<pcf_mc_request>& synthetic, Edit edit,
+              bool applies = true) {
     const std::vector<pcf_mc_request>& reqs = user.empty() ? synthetic : user;
-    if (st || reqs.empty()) return;
-    double t_cur = -1, t_best = 1e30;
+    if (st || reqs.empty() || (!user.empty() && !applies)) return;
+    double t_cur = 1e30, t_best = 1e30;
     int best = current;
     char buf[160];
-    for (int v : cands) {
+    std::vector<int> order{current};
+    for (int v : cands)
+      if (v != current) order.push_back(v);
+    order.push_back(current);
+    for (int v : order) {
       TuneTable x = t;
       edit(x, v);
       tune_set(dev, x);
@@ -321,14 +330,26 @@ struct Tuner {
       snprintf(buf, sizeof buf, "%s{\"knob\": \"%s\", \"value\": %d, \"ms\": %.5f}",
                trials.empty() ? "" : ", ", what, v, ms);
       trials += buf;
-      if (v == current) t_cur = ms;
-      if (ms < t_best) {
+      if (v == current) {
+        t_cur = std::min(t_cur, ms);
+      } else if (ms < t_best) {
         t_best = ms;
         best = v;
       }
     }
-    if (!st && best != current && (t_cur < 0 || t_best < 0.98 * t_cur)) edit(t, best);
+    if (!st && best != current && t_best < 0.98 * t_cur) edit(t, best);
     tune_set(dev, t);
+  }
+
+  // What the caller's batch holds, for `applies`: a request of `method` with
+  // N in [nlo, nhi) and M (baskets: d) in [mlo, mhi].
+  bool has(int method, long long nlo = 0, long long nhi = (1LL << 62), int mlo = 0,
+           int mhi = 1 << 30) const {
+    for (const pcf_mc_request& q : user) {
+      const int m = method == PCF_METHOD_BASKET ? q.assets : q.M;
+      if (q.method == method && q.N >= nlo && q.N < nhi && m >= mlo && m <= mhi) return true;
+    }
+    return false;
   }
 };
 
@@ -369,12 +390,16 @@ int run_tuner(pcf_ctx* c, int flags, const pcf_mc_request* ureqs, int un, char* 
       auto b = batch(PCF_METHOD_EUR, eC[k], eN[k], 0, 0);
       all.insert(all.end(), b.begin(), b.end());
     }
-    tu.choose("eur_block", blocks, tu.t.eur_block, all, [](TuneTable& x, int v) { x.eur_block = v; });
+    const long long eLo[4] = {0, 1LL << 18, 1LL << 22, 1LL << 26};
+    const long long eHi[4] = {1LL << 18, 1LL << 22, 1LL << 26, 1LL << 62};
+    tu.choose("eur_block", blocks, tu.t.eur_block, all, [](TuneTable& x, int v) { x.eur_block = v; },
+              tu.has(PCF_METHOD_EUR));
     for (int k = 0; k < 4; ++k) {
       char w[32];
       snprintf(w, sizeof w, "eur_items[%d]", k);
       tu.choose(w, {8, 16, 32, 64, 128}, tu.t.eur_items[k], batch(PCF_METHOD_EUR, eC[k], eN[k], 0, 0),
-                [k](TuneTable& x, int v) { x.eur_items[k] = v; });
+                [k](TuneTable& x, int v) { x.eur_items[k] = v; },
+                tu.has(PCF_METHOD_EUR, eLo[k], eHi[k]));
     }
     // Asian: classes of M represented by 12, 52, 252 and 1000 steps.
     const int aM[4] = {12, 52, 252, 1000};
@@ -384,30 +409,35 @@ int run_tuner(pcf_ctx* c, int flags, const pcf_mc_request* ureqs, int un, char* 
       auto b = batch(PCF_METHOD_ASIA, aC[k], 1LL << 17, aM[k], 0);
       all.insert(all.end(), b.begin(), b.end());
     }
-    tu.choose("asia_block", blocks, tu.t.asia_block, all, [](TuneTable& x, int v) { x.asia_block = v; });
+    const int aLo[4] = {0, 17, 65, 257}, aHi[4] = {16, 64, 256, 1 << 30};
+    tu.choose("asia_block", blocks, tu.t.asia_block, all,
+              [](TuneTable& x, int v) { x.asia_block = v; }, tu.has(PCF_METHOD_ASIA));
     for (int k = 0; k < 4; ++k) {
       char w[32];
       snprintf(w, sizeof w, "asia_steps[%d]", k);
       tu.choose(w, {128, 256, 512, 1024, 2048}, tu.t.asia_steps[k],
                 batch(PCF_METHOD_ASIA, aC[k], 1LL << 17, aM[k], 0),
-                [k](TuneTable& x, int v) { x.asia_steps[k] = v; });
+                [k](TuneTable& x, int v) { x.asia_steps[k] = v; },
+                tu.has(PCF_METHOD_ASIA, 0, 1LL << 62, aLo[k], aHi[k]));
     }
     // Baskets: 4, 8, 16 assets on the CUDA cores, 32 and 64 on the tensor cores.
     const int bD[5] = {4, 8, 16, 32, 64};
+    const int bLo[5] = {1, 5, 9, 17, 33};
     for (int k = 0; k < 5; ++k) {
       const auto b = batch(PCF_METHOD_BASKET, k < 3 ? 8 : 4, 1LL << 20, 0, bD[k]);
+      const bool here = tu.has(PCF_METHOD_BASKET, 0, 1LL << 62, bLo[k], bD[k]);
       char w[32];
       if (k < 3) {
         snprintf(w, sizeof w, "basket_block[%d]", k);
         tu.choose(w, blocks, tu.t.basket_block[k], b,
-                  [k](TuneTable& x, int v) { x.basket_block[k] = v; });
+                  [k](TuneTable& x, int v) { x.basket_block[k] = v; }, here);
         snprintf(w, sizeof w, "basket_ppt[%d]", k);
         tu.choose(w, {2, 4, 8, 16, 32}, tu.t.basket_ppt[k], b,
-                  [k](TuneTable& x, int v) { x.basket_ppt[k] = v; });
+                  [k](TuneTable& x, int v) { x.basket_ppt[k] = v; }, here);
       } else {
         snprintf(w, sizeof w, "tc_tiles[%d]", k - 3);
         tu.choose(w, {2, 4, 8, 16, 32}, tu.t.tc_tiles[k - 3], b,
-                  [k](TuneTable& x, int v) { x.tc_tiles[k - 3] = v; });
+                  [k](TuneTable& x, int v) { x.tc_tiles[k - 3] = v; }, here);
       }
     }
     // 17 to 32 assets: the CUDA-core kernel (its shape first) against the
@@ -415,13 +445,14 @@ int run_tuner(pcf_ctx* c, int flags, const pcf_mc_request* ureqs, int un, char* 
     // from the smallest one from which on they win at each size timed. On
     // the caller's batch, the threshold itself is the knob.
     const auto b24 = batch(PCF_METHOD_BASKET, 4, 1LL << 20, 0, 24);
+    const bool mid = tu.has(PCF_METHOD_BASKET, 0, 1LL << 62, 17, 32);
     tu.choose("basket_ppt[3]", {2, 4, 8, 16}, tu.t.basket_ppt[3], b24,
-              [](TuneTable& x, int v) { x.basket_ppt[3] = v; x.tc_min_d = 33; });
+              [](TuneTable& x, int v) { x.basket_ppt[3] = v; x.tc_min_d = 33; }, mid);
     tu.t.tc_min_d = before.tc_min_d;  // the edit above timed the CUDA-core route only
     tune_set(c->device, tu.t);
     if (!tu.user.empty()) {
       tu.choose("tc_min_d", {17, 20, 24, 28, 33}, tu.t.tc_min_d, {},
-                [](TuneTable& x, int v) { x.tc_min_d = v; });
+                [](TuneTable& x, int v) { x.tc_min_d = v; }, mid);
     } else {
       const int dset[5] = {17, 20, 24, 28, 32};
       bool tc_wins[5];
@@ -456,8 +487,11 @@ int run_tuner(pcf_ctx* c, int flags, const pcf_mc_request* ureqs, int un, char* 
       const int count = N <= (1 << 16) ? 64 : N <= (1 << 18) ? 32 : N <= (1 << 20) ? 16 : 8;
       char w[32];
       snprintf(w, sizeof w, "lsm_shift[%d]", k);
+      const long long lo = 1LL << (14 + k);
+      const long long hi = k == kTuneLsmClasses - 1 ? (1LL << 62) : 1LL << (15 + k);
       tu.choose(w, {-1, 0, 1}, tu.t.lsm_shift[k], batch(PCF_METHOD_AMER, count, N, 50, 0),
-                [k](TuneTable& x, int v) { x.lsm_shift[k] = v; });
+                [k](TuneTable& x, int v) { x.lsm_shift[k] = v; },
+                tu.has(PCF_METHOD_AMER, lo, hi));
     }
   }
   if (tu.st) {

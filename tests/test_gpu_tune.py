@@ -117,3 +117,25 @@ def test_autotune_then_results_hold_and_reset(orc, ctx):
     t = ctx.tuning()["table"]
     assert not t["tuned"] and t["eur_block"] == 256 and t["basket_ppt"] == [16, 8, 8, 4]
     assert t["tc_min_d"] == 17
+
+
+def test_autotune_on_a_batch_tunes_only_what_the_batch_uses(orc, ctx):
+    """pcf_autotune_batch times every knob on the caller's batch and leaves
+    alone the knobs that shape none of it (European-only batch: no Asian,
+    basket or American knob is timed); prices stay at the twins' values."""
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("eur", 100, 90 + 2 * k, .05, .2, 1.0, 1 << 20, "call", seed=9, stream=k)
+            for k in range(16)]
+    try:
+        rep = ctx.autotune(requests=reqs)
+        assert rep["mode"] == "batch"
+        knobs = {x["knob"] for x in rep["trials"]}
+        assert "eur_block" in knobs and "eur_items[1]" in knobs
+        assert not any(k.startswith(("asia", "basket", "tc_", "lsm")) for k in knobs), knobs
+        out = pcf.price_batch(reqs, ctx=ctx)
+        s = (C.c_double * 6)()
+        for k in (0, 15):
+            orc.twin_mc_eur(100, 90 + 2 * k, .05, .2, 1.0, 1 << 20, 1, 9, k, s)
+            assert abs(out[k].sums[0] - s[0]) < 1e-5 * s[0]
+    finally:
+        ctx.tune_reset()
