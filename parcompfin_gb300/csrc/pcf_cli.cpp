@@ -27,8 +27,11 @@
 //                        in the working directory (the reference's run
 //                        scripts write that file), else 0
 //   PCF_SEED             Philox seed; default time(NULL), like the reference
-//   PCF_REF_EXERCISE=1   mc_amer: the reference's exercise rule
-//                        (src/mc_amer.cpp:100); default: correct LSM
+//   PCF_REF_EXERCISE     mc_amer: unset or 1 (the default) keeps the
+//                        reference's exercise rule (src/mc_amer.cpp:100),
+//                        so the program prints what the reference's prints
+//                        (about 94 for an at-the-money put); 0 exercises at
+//                        payoff(S), correct Longstaff-Schwartz
 //   PCF_CV=1             report the control-variate estimate
 //   PCF_BINOM_MODE=1     binom_embar: accurate weights; default 0 reproduces
 //                        the reference's rounding
@@ -81,9 +84,10 @@ bool arg_i(char** argv, int argc, int idx, long long* out) {
   return end != argv[idx];
 }
 
-bool env_flag(const char* name) {
+bool env_flag(const char* name, bool dflt = false) {
   const char* v = getenv(name);
-  return v && *v && strcmp(v, "0") != 0;
+  if (!v || !*v) return dflt;
+  return strcmp(v, "0") != 0;
 }
 
 double comparison_value() {
@@ -229,7 +233,7 @@ int main(int argc, char** argv) {
   } else if (stem == "mc_asia") {
     st = pcf_mc_asia(ctx, S0, E, r, sigma, T, N, (int)M, pf, 0, seed, cv, &res);
   } else if (stem == "mc_amer") {
-    st = pcf_mc_amer(ctx, S0, E, r, sigma, T, N, (int)M, pf, env_flag("PCF_REF_EXERCISE"), seed,
+    st = pcf_mc_amer(ctx, S0, E, r, sigma, T, N, (int)M, pf, env_flag("PCF_REF_EXERCISE", true), seed,
                      cv, &res);
   } else if (stem == "binom_embar") {
     st = pcf_binom_embar(ctx, S0, E, r, sigma, T, (int)N, pf, env_flag("PCF_BINOM_MODE"),

@@ -63,8 +63,15 @@ def test_asia_amer_multi_match_the_c_abi():
     assert row["M"] == "52"
     assert float(row["Result"]) == pcf.mc_asia_result(100, 100, .04, .3, 1.5, 40000, 52, "call",
                                                       seed=7).price_plain
+    # The drop-in mc_amer keeps the reference's exercise rule by default
+    # (its put prints ~94, as the reference's program does); PCF_REF_EXERCISE=0
+    # selects correct Longstaff-Schwartz.
     row = run("mc_amer", "put", 100, 100, .05, .3, 1, 20000, 50)
     assert row["M"] == "50"
+    assert float(row["Result"]) == pcf.mc_amer_result(100, 100, .05, .3, 1.0, 20000, 50, "put",
+                                                      ref_exercise=True, seed=7).price_plain
+    assert float(row["Result"]) > 50
+    row = run("mc_amer", "put", 100, 100, .05, .3, 1, 20000, 50, PCF_REF_EXERCISE=0)
     assert float(row["Result"]) == pcf.mc_amer_result(100, 100, .05, .3, 1.0, 20000, 50, "put",
                                                       seed=7).price_plain
     row = run("mc_eur_multi", "call", 100, 100, .1, .2, 1, 200000, 4, .5)
