@@ -86,11 +86,11 @@ def _fp32_roofline(flop_per_unit, units, ms, sms, sm_mhz):
 # --------------------------------------------------------------------------
 # workloads
 # --------------------------------------------------------------------------
-# DRAM bytes per algorithmic byte of the American cluster kernel: one
-# `ncu --set full` capture of the 64-put batch (dram__bytes_read.sum +
-# dram__bytes_write.sum = 1635.3 MB for 1677.7 MB algorithmic;
-# profiles/lsm_cluster_kernel_64_puts_2p16.md). Traffic grows with the
-# path-dates, so other launches of the kernel scale by it.
+# DRAM bytes per algorithmic byte of the American cluster kernel, from one
+# `ncu --set full` capture of its launch on the amerbatch workload (64 puts,
+# 2^16 paths, 50 dates; dram__bytes_read.sum + dram__bytes_write.sum =
+# 1635.3 MB for 1677.7 MB algorithmic). Traffic grows with the path-dates, so
+# other launches of the kernel scale by it.
 LSM_TRAFFIC_PER_ALG_BYTE = 1635.3 / 1677.7
 
 
