@@ -15,10 +15,11 @@
 // The kernels are issue-bound (a European path is ~31 FP32/INT instructions,
 // two thirds of them Philox and Box-Muller, against 3 SFU operations), so the
 // control-variate sums are compiled in only when a launch asks for them (CV
-// template flag). Baskets of 17 to 64 assets run mc_basket_tc_kernel, which
-// multiplies the normals by the correlation factor on the tensor cores, from
-// the basket size the tuning table routes there (17 to 32 assets can also
-// run the CUDA-core kernel; above 32 they always take the tensor cores).
+// template flag). Baskets of more than 16 assets run mc_basket_tc_kernel,
+// which multiplies the normals by the correlation factor on the tensor
+// cores, from the basket size the tuning table routes there (24 built in,
+// where the tensor cores start to win; below it, up to 32 assets, the
+// CUDA-core kernel runs; above 32 the tensor cores always do).
 //
 // Reference loops these kernels replace:
 //   European  src/mc_eur.cpp:22-26,  src/mc_eur_omp.cpp:24-27

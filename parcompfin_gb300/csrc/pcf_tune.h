@@ -30,7 +30,10 @@ struct TuneTable {
   int basket_block[4] = {256, 256, 256, 256};
   int basket_ppt[4] = {16, 8, 8, 4};  // paths per thread per item
   int tc_tiles[2] = {8, 8};           // 128-path tiles per item, tensor-core kernel (d <= 32, <= 64)
-  int tc_min_d = 17;                  // baskets of at least this many assets take the tensor cores
+  // Baskets of at least this many assets take the tensor cores: measured at
+  // 2^21 paths, the CUDA cores win at 17 and 20 assets, the tensor cores from
+  // 24 on.
+  int tc_min_d = 24;
   // Longstaff-Schwartz cluster launch: 0 takes the smallest cluster whose
   // CTAs cover the contract two to an SM; +1 doubles the cluster (half the
   // slice), -1 halves it (twice the slice, one CTA per SM if it must).

@@ -158,7 +158,8 @@ def _chol(corr, d):
     return L
 
 
-# d > 16 runs the tensor-core kernel (3xTF32 products): 17, 24 and 48 leave
+# From 24 assets the tensor-core kernel runs (3xTF32 products; 17 to 23 run
+# the CUDA-core kernel for up to 32 assets): 17, 24 and 48 leave
 # padded K and N, 32 and 64 fill them exactly.
 @pytest.mark.parametrize("d", [1, 4, 7, 16, 17, 24, 32, 33, 48, 64])
 def test_basket_matches_fp64_twin(orc, ctx, d):

@@ -116,7 +116,7 @@ def test_autotune_then_results_hold_and_reset(orc, ctx):
         ctx.tune_reset()
     t = ctx.tuning()["table"]
     assert not t["tuned"] and t["eur_block"] == 256 and t["basket_ppt"] == [16, 8, 8, 4]
-    assert t["tc_min_d"] == 17
+    assert t["tc_min_d"] == 24
 
 
 def test_autotune_on_a_batch_tunes_only_what_the_batch_uses(orc, ctx):
