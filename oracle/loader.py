@@ -47,6 +47,9 @@ SIGS = {
     "twin_mc_asia": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _I, _U64, _U32, _PD]),
     "twin_mc_basket": (None, [_I, _PD, _PD, _PD, _D, _D, _D, _D, _I64, _I, _U64, _U32, _PD]),
     "twin_mc_amer": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _I, _U64, _U32, _PD]),
+    "orc_emulate_lsm_record": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _U64, _U32,
+                                      C.POINTER(C.c_float), _PD, C.POINTER(C.c_uint16),
+                                      C.POINTER(C.c_float), _PD]),
     "twin_mc_amer_audit": (None, [_D, _D, _D, _D, _D, _I64, _I, _I, _I, _U64, _U32,
                                   C.POINTER(C.c_float), _PD, C.POINTER(C.c_uint16),
                                   C.POINTER(C.c_float), _PD, _PD]),

@@ -1202,3 +1202,78 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
   rep[27] = first4_margin;
   rep[28] = first4_fitdiff;
 }
+
+/* An audit record as the kernel would write it, made on the CPU: the FP64
+ * paths rounded to FP32, the kernel's sweep replayed in FP32 (its decision
+ * formulas, fmaf included), each date's coefficients from an FP64
+ * regression of that state rounded to FP32. It feeds twin_mc_amer_audit in
+ * the CPU tests, clean and with planted mistakes, to show the audit accepts
+ * a consistent record and catches a wrong one. gcoef[M*4], gsums[M*8],
+ * gtau[N], gu[M*N], gmom[5] as pcf_mc_amer_audit's (ref_exercise = 0). */
+ORC_EXPORT void orc_emulate_lsm_record(double S0, double E, double r, double sigma, double T,
+                                       int64_t N, int M, int pf, uint64_t seed, uint32_t stream,
+                                       float* gcoef, double* gsums, uint16_t* gtau, float* gu,
+                                       double* gmom) {
+  const int64_t H = N / 2;
+  const double dtd = T / M, sdt = sqrt(dtd), nu_dt = (r - 0.5 * sigma * sigma) * dtd;
+  for (int64_t p = 0; p < H; ++p) {
+    double lp = 0, lm = 0, z[4] = {0, 0, 0, 0};
+    for (int m = 1; m <= M; ++m) {
+      if ((m - 1) % 4 == 0) orc::normals4(seed, stream, 4u, (uint64_t)p, (uint32_t)((m - 1) / 4), z);
+      const double zm = z[(m - 1) % 4];
+      lp += nu_dt + sigma * sdt * zm;
+      lm += nu_dt - sigma * sdt * zm;
+      gu[(size_t)(m - 1) * N + p] = (float)(pf * (S0 * exp(lp) / E - 1.0));
+      gu[(size_t)(m - 1) * N + p + H] = (float)(pf * (S0 * exp(lm) / E - 1.0));
+    }
+  }
+  std::vector<float> dtf((size_t)M + 1), edtf((size_t)M + 1);
+  for (int k = 0; k <= M; ++k) {
+    dtf[k] = (float)exp(-r * dtd * k);
+    edtf[k] = (float)exp(r * dtd * k);
+  }
+  const float Ef = (float)E, EdM = Ef * dtf[M];
+  std::vector<float> cf((size_t)N);
+  for (int64_t n = 0; n < N; ++n) {
+    cf[n] = fmaxf(gu[(size_t)(M - 1) * N + n], 0.f) * EdM;
+    gtau[n] = (uint16_t)M;
+  }
+  for (int k = 0; k < 4 * M; ++k) gcoef[k] = 0.f;
+  for (int k = 0; k < 8 * M; ++k) gsums[k] = 0.0;
+  for (int m = M - 1; m >= 1; --m) {
+    const float* u = gu + (size_t)(m - 1) * N;
+    double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t n = 0; n < N; ++n)
+      if (u[n] > 0.f) {
+        const double x = u[n], y = cf[n];
+        a[0] += 1; a[1] += x; a[2] += x * x; a[3] += x * x * x; a[4] += x * x * x * x;
+        a[5] += y; a[6] += y * x; a[7] += y * x * x;
+      }
+    for (int k = 5; k < 8; ++k) a[k] *= (double)edtf[m];
+    for (int k = 0; k < 8; ++k) gsums[(size_t)m * 8 + k] = a[k];
+    double c[3];
+    const int mode = solve_mode(a, c);
+    const float c0 = (float)c[0], c1 = (float)c[1], c2 = (float)c[2];
+    gcoef[(size_t)m * 4] = (float)mode;
+    gcoef[(size_t)m * 4 + 1] = c0;
+    gcoef[(size_t)m * 4 + 2] = c1;
+    gcoef[(size_t)m * 4 + 3] = c2;
+    if (mode == 0) continue;
+    for (int64_t n = 0; n < N; ++n) {
+      const float uf = u[n];
+      if (!(uf > 0.f)) continue;
+      const float ex = uf * Ef;
+      const float cont = mode == 1 ? cf[n] * edtf[m] : fmaf(fmaf(c2, uf, c1), uf, c0);
+      if (ex > cont) {
+        cf[n] = ex * dtf[m];
+        gtau[n] = (uint16_t)m;
+      }
+    }
+  }
+  double s[5] = {0, 0, 0, 0, 0};
+  for (int64_t p = 0; p < H; ++p) {
+    const double y = 0.5 * ((double)cf[p] + (double)cf[p + H]);
+    s[0] += y; s[1] += y * y;
+  }
+  for (int k = 0; k < 5; ++k) gmom[k] = s[k];
+}
