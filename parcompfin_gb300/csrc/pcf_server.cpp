@@ -38,6 +38,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <exception>
 #include <functional>
 #include <mutex>
 #include <thread>
@@ -627,7 +628,12 @@ extern "C" int pcf_server_start(pcf_ctx* ctx, const pcf_server_config* cfg_in,
     return st;
   }
   s->t0 = Clock::now();
-  s->worker = std::thread(serve_worker, s);
+  try {
+    s->worker = std::thread(serve_worker, s);
+  } catch (const std::exception& e) {  // no C++ exception crosses the ABI
+    delete s;
+    return set_error(PCF_EINVAL, "cannot start the server's worker thread: %s", e.what());
+  }
   *out = s;
   return PCF_OK;
 }

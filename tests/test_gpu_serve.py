@@ -14,6 +14,7 @@
   * requests arriving while other batches run are admitted into other slots
     (more than one batch in flight).
 """
+import ctypes as C
 import math
 
 import pytest
@@ -227,3 +228,34 @@ def test_live_server_admits_while_running_and_matches_alone(ctx):
             for a, b in zip(alone.sums, out[i].result.sums):
                 assert abs(a - b) <= 1e-8 * max(abs(a), abs(b)), (q, a, b)
     assert continued > 0
+
+
+def test_empty_inputs(ctx):
+    """An empty trace, and a live server that serves nothing, finish with
+    nothing completed; an empty batch prices nothing."""
+    import parcompfin_gb300 as pcf
+    out, st = pcf.serve_trace([], [], target_rel_se=TARGET, ctx=ctx)
+    assert out == [] and st.completed == 0
+    srv = pcf.Server(ctx, target_rel_se=TARGET)
+    stats = srv.stop()
+    assert stats.completed == 0
+    assert pcf.price_batch([], ctx=ctx) == []
+
+
+def test_smallest_contracts_in_one_batch(orc, ctx):
+    """One path (European, Asian, basket) and one antithetic pair (American)
+    in one batch: every result is finite and equals the contract alone."""
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("eur", 100, 100, .05, .2, 1.0, 1, "call", seed=1, stream=0),
+            pcf.request("asia", 100, 100, .04, .3, 1.0, 1, "put", M=7, seed=1, stream=1),
+            pcf.request("basket", 100, 100, .03, .25, 1.0, 1, "call", assets=5, rho=.2,
+                        seed=1, stream=2),
+            pcf.request("amer", 100, 110, .05, .3, 1.0, 2, "put", M=3, seed=1, stream=3)]
+    out = pcf.price_batch(reqs, ctx=ctx)
+    for q, r in zip(reqs, out):
+        assert r.n_paths == q["N"] and math.isfinite(r.price), (q, r.price)
+        alone = pcf.price_batch([q], ctx=ctx)[0]
+        assert list(alone.sums) == list(r.sums)
+    s = (C.c_double * 6)()
+    orc.twin_mc_eur(100, 100, .05, .2, 1.0, 1, 1, 1, 0, s)
+    assert abs(out[0].sums[0] - s[0]) <= 1e-5 * max(abs(s[0]), 1e-9)
