@@ -390,8 +390,11 @@ PCF_API int pcf_server_poll(pcf_server* srv, long long ticket, pcf_served_result
 PCF_API int pcf_server_wait(pcf_server* srv, long long ticket, double timeout_s,
                             pcf_served_result* out);
 /* Finishes every submitted request, stops the worker, fills stats over all
- * requests served and frees the server (the slots stay with the context).
- * Returns the first batch error, if any. */
+ * requests served and frees the server (the slots stay with the context)
+ * once every submit, poll or wait call already in progress on other threads
+ * has returned (a submit that arrives meanwhile is refused). No call may
+ * start on the handle after pcf_server_stop has returned. Returns the first
+ * batch error, if any. */
 PCF_API int pcf_server_stop(pcf_server* srv, pcf_server_stats* stats);
 
 #ifdef __cplusplus

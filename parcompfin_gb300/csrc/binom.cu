@@ -450,72 +450,76 @@ using namespace pcf;
 
 extern "C" int pcf_binom_embar_batch(pcf_ctx* ctx, int n, const pcf_binom_contract* ks, int mode,
                                      double* prices) {
-  if (n < 0 || (n > 0 && (!ks || !prices))) return set_error(PCF_EINVAL, "bad arguments");
-  if (mode != 0 && mode != 1) return set_error(PCF_EINVAL, "mode must be 0 or 1");
-  if (n == 0) return PCF_OK;
-  std::vector<BinomContract> cs((size_t)n);
-  int nmax = 1;
-  for (int i = 0; i < n; ++i) {
-    int st = setup_contract(ks[i], i, cs[i]);
+  return pcf::abi_guard([&]() -> int {
+    if (n < 0 || (n > 0 && (!ks || !prices))) return set_error(PCF_EINVAL, "bad arguments");
+    if (mode != 0 && mode != 1) return set_error(PCF_EINVAL, "mode must be 0 or 1");
+    if (n == 0) return PCF_OK;
+    std::vector<BinomContract> cs((size_t)n);
+    int nmax = 1;
+    for (int i = 0; i < n; ++i) {
+      int st = setup_contract(ks[i], i, cs[i]);
+      if (st) return st;
+      nmax = std::max(nmax, ks[i].N);
+    }
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    st = ensure_tables(c, nmax);
     if (st) return st;
-    nmax = std::max(nmax, ks[i].N);
-  }
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  st = ensure_tables(c, nmax);
-  if (st) return st;
-  std::vector<int> start((size_t)n + 1, 0);
-  for (int i = 0; i < n; ++i) start[i + 1] = start[i] + cs[i].items;
-  const int items = start[n];
-  const size_t o_cs = 0;
-  const size_t o_start = a256(sizeof(BinomContract) * n);
-  const size_t h2d = a256(o_start + sizeof(int) * (n + 1));
-  const size_t o_part = h2d;
-  const size_t o_tick = a256(o_part + sizeof(double) * items);
-  const size_t o_out = a256(o_tick + sizeof(unsigned) * n);
-  const size_t total = a256(o_out + sizeof(double) * n);
-  st = ctx_ensure(c, total, std::max(h2d, sizeof(double) * n));
-  if (st) return st;
-  char* h = (char*)c->h_buf;
-  char* d = (char*)c->d_buf;
-  memcpy(h + o_cs, cs.data(), sizeof(BinomContract) * n);
-  memcpy(h + o_start, start.data(), sizeof(int) * (n + 1));
-  st = cuda_status(cudaMemcpyAsync(d, h, h2d, cudaMemcpyHostToDevice, c->stream), "H2D binom");
-  if (!st) st = cuda_status(cudaMemsetAsync(d + o_tick, 0, sizeof(unsigned) * n, c->stream),
-                            "memset binom tickets");
-  if (st) return st;
-  BinomLaunch L;
-  L.cs = (const BinomContract*)(d + o_cs);
-  L.item_start = (const int*)(d + o_start);
-  L.ncontracts = n;
-  L.total_items = items;
-  L.partial = (double*)(d + o_part);
-  L.tickets = (unsigned*)(d + o_tick);
-  L.out = (double*)(d + o_out);
-  L.mode = mode;
-  char* tb = (char*)c->d_logtab;
-  L.t.logt = (const double*)tb;
-  L.t.pref = (const unsigned long long*)(tb + c->binom_off[0]);
-  L.t.tie_off = (const int*)(tb + c->binom_off[1]);
-  L.t.tie_pos = (const int*)(tb + c->binom_off[2]);
-  L.stirl = (const double*)(tb + c->binom_off[3]);
-  L.t.nmax = c->logtab_n;
-  binom_kernel<<<items, kBinomBlock, 0, c->stream>>>(L);
-  st = cuda_status(cudaGetLastError(), "binom kernel launch");
-  if (st) return st;
-  c->launches += 1;
-  st = cuda_status(cudaMemcpyAsync(h, L.out, sizeof(double) * n, cudaMemcpyDeviceToHost,
-                                   c->stream), "D2H binom");
-  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "binom kernel");
-  if (st) return st;
-  for (int i = 0; i < n; ++i) prices[i] = exp(-ks[i].r * ks[i].T) * ((double*)h)[i];  // :49
-  return PCF_OK;
+    std::vector<int> start((size_t)n + 1, 0);
+    for (int i = 0; i < n; ++i) start[i + 1] = start[i] + cs[i].items;
+    const int items = start[n];
+    const size_t o_cs = 0;
+    const size_t o_start = a256(sizeof(BinomContract) * n);
+    const size_t h2d = a256(o_start + sizeof(int) * (n + 1));
+    const size_t o_part = h2d;
+    const size_t o_tick = a256(o_part + sizeof(double) * items);
+    const size_t o_out = a256(o_tick + sizeof(unsigned) * n);
+    const size_t total = a256(o_out + sizeof(double) * n);
+    st = ctx_ensure(c, total, std::max(h2d, sizeof(double) * n));
+    if (st) return st;
+    char* h = (char*)c->h_buf;
+    char* d = (char*)c->d_buf;
+    memcpy(h + o_cs, cs.data(), sizeof(BinomContract) * n);
+    memcpy(h + o_start, start.data(), sizeof(int) * (n + 1));
+    st = cuda_status(cudaMemcpyAsync(d, h, h2d, cudaMemcpyHostToDevice, c->stream), "H2D binom");
+    if (!st) st = cuda_status(cudaMemsetAsync(d + o_tick, 0, sizeof(unsigned) * n, c->stream),
+                              "memset binom tickets");
+    if (st) return st;
+    BinomLaunch L;
+    L.cs = (const BinomContract*)(d + o_cs);
+    L.item_start = (const int*)(d + o_start);
+    L.ncontracts = n;
+    L.total_items = items;
+    L.partial = (double*)(d + o_part);
+    L.tickets = (unsigned*)(d + o_tick);
+    L.out = (double*)(d + o_out);
+    L.mode = mode;
+    char* tb = (char*)c->d_logtab;
+    L.t.logt = (const double*)tb;
+    L.t.pref = (const unsigned long long*)(tb + c->binom_off[0]);
+    L.t.tie_off = (const int*)(tb + c->binom_off[1]);
+    L.t.tie_pos = (const int*)(tb + c->binom_off[2]);
+    L.stirl = (const double*)(tb + c->binom_off[3]);
+    L.t.nmax = c->logtab_n;
+    binom_kernel<<<items, kBinomBlock, 0, c->stream>>>(L);
+    st = cuda_status(cudaGetLastError(), "binom kernel launch");
+    if (st) return st;
+    c->launches += 1;
+    st = cuda_status(cudaMemcpyAsync(h, L.out, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                     c->stream), "D2H binom");
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "binom kernel");
+    if (st) return st;
+    for (int i = 0; i < n; ++i) prices[i] = exp(-ks[i].r * ks[i].T) * ((double*)h)[i];  // :49
+    return PCF_OK;
+  });
 }
 
 extern "C" int pcf_binom_embar(pcf_ctx* ctx, double S0, double E, double r, double sigma,
                                double T, int N, int payoff_fun, int mode, double* price) {
-  if (!price) return set_error(PCF_EINVAL, "price is NULL");
-  pcf_binom_contract k{S0, E, r, sigma, T, N, payoff_fun};
-  return pcf_binom_embar_batch(ctx, 1, &k, mode, price);
+  return pcf::abi_guard([&]() -> int {
+    if (!price) return set_error(PCF_EINVAL, "price is NULL");
+    pcf_binom_contract k{S0, E, r, sigma, T, N, payoff_fun};
+    return pcf_binom_embar_batch(ctx, 1, &k, mode, price);
+  });
 }

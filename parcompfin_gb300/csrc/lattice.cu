@@ -137,90 +137,92 @@ using namespace pcf;
 
 extern "C" int pcf_binom_vanilla(pcf_ctx* ctx, double S0, double E, double r, double sigma,
                                  double T, int N, int payoff_fun, int american, double* price) {
-  if (!price) return set_error(PCF_EINVAL, "price is NULL");
-  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
-  if (st) return st;
-  if (N > kLatMaxN) return set_error(PCF_EINVAL, "N must be <= %d", kLatMaxN);
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  double u, d, p, q, R;
-  lattice(r, sigma, T, N, u, d, p, q, R);
+  return pcf::abi_guard([&]() -> int {
+    if (!price) return set_error(PCF_EINVAL, "price is NULL");
+    int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+    if (st) return st;
+    if (N > kLatMaxN) return set_error(PCF_EINVAL, "N must be <= %d", kLatMaxN);
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    double u, d, p, q, R;
+    lattice(r, sigma, T, N, u, d, p, q, R);
 
-  int G = N > kLatTail ? std::min(c->sm_count, (N + 1 + 511) / 512) : 1;
-  G = std::max(G, 1);
-  const int seg_cap = (N + 1 + G - 1) / G;
-  const size_t smem = sizeof(double) * (size_t)std::max(2 * (seg_cap + kLatSteps),
-                                                        2 * (kLatTail + 1));
-  st = cuda_status(cudaFuncSetAttribute(lattice_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                   "lattice smem attribute");
-  if (st) return st;
-  int occ = 0;
-  st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lattice_kernel, kLatBlock,
-                                                                 smem),
-                   "occupancy(lattice)");
-  if (st) return st;
-  if ((long long)occ * c->sm_count < G)
-    return set_error(PCF_EINVAL, "lattice grid of %d blocks cannot be co-resident", G);
+    int G = N > kLatTail ? std::min(c->sm_count, (N + 1 + 511) / 512) : 1;
+    G = std::max(G, 1);
+    const int seg_cap = (N + 1 + G - 1) / G;
+    const size_t smem = sizeof(double) * (size_t)std::max(2 * (seg_cap + kLatSteps),
+                                                          2 * (kLatTail + 1));
+    st = cuda_status(cudaFuncSetAttribute(lattice_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                     "lattice smem attribute");
+    if (st) return st;
+    int occ = 0;
+    st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lattice_kernel, kLatBlock,
+                                                                   smem),
+                     "occupancy(lattice)");
+    if (st) return st;
+    if ((long long)occ * c->sm_count < G)
+      return set_error(PCF_EINVAL, "lattice grid of %d blocks cannot be co-resident", G);
 
-  // Scratch: up | dn | A | B | counters (barrier, err) | out.
-  const size_t nodes = (size_t)N + 1;
-  const size_t o_up = 0, o_dn = o_up + 8 * nodes, o_A = o_dn + 8 * nodes, o_B = o_A + 8 * nodes;
-  const size_t o_cnt = (o_B + 8 * nodes + 255) & ~(size_t)255;
-  const size_t o_out = o_cnt + 256;
-  const size_t total = o_out + 256;
-  st = ctx_ensure(c, total, 16 * nodes + 64);
-  if (st) return st;
-  char* dv = (char*)c->d_buf;
-  double* h = (double*)c->h_buf;
-  // The reference's pow(u, i) and pow(d, n - i) (src/binom_vanilla_amer.cpp:28,32).
-  for (size_t i = 0; i < nodes; ++i) {
-    h[i] = pow(u, (double)i);
-    h[nodes + i] = pow(d, (double)i);
-  }
-  st = cuda_status(cudaMemcpyAsync(dv + o_up, h, 16 * nodes, cudaMemcpyHostToDevice, c->stream),
-                   "H2D lattice tables");
-  if (!st)
-    st = cuda_status(cudaMemsetAsync(dv + o_cnt, 0, 256, c->stream), "memset lattice counters");
-  if (st) return st;
-  LatticeParams P;
-  memset(&P, 0, sizeof P);
-  P.S0 = S0;
-  P.E = E;
-  P.p = p;
-  P.q = q;
-  P.R = R;
-  P.N = N;
-  P.pf = payoff_fun;
-  P.american = american ? 1 : 0;
-  P.up = (const double*)(dv + o_up);
-  P.dn = (const double*)(dv + o_dn);
-  P.A = (double*)(dv + o_A);
-  P.B = (double*)(dv + o_B);
-  P.barrier = (unsigned*)(dv + o_cnt);
-  P.err = (int*)(dv + o_cnt + 64);
-  P.wait_limit = 1u << 22;
-  if (c->test_barrier_extra) {  // test hook: a barrier that cannot complete
-    P.barrier_extra = c->test_barrier_extra;
-    P.wait_limit = c->test_poll_limit;
-  }
-  P.out = (double*)(dv + o_out);
-  int cap = seg_cap;
-  void* args[] = {&P, &cap};
-  st = cuda_status(cudaLaunchCooperativeKernel((void*)lattice_kernel, dim3(G), dim3(kLatBlock),
-                                               args, smem, c->stream),
-                   "lattice kernel launch");
-  if (st) return st;
-  c->launches += 1;
-  st = cuda_status(cudaMemcpyAsync(h, dv + o_out, 8, cudaMemcpyDeviceToHost, c->stream),
-                   "D2H lattice");
-  if (!st)
-    st = cuda_status(cudaMemcpyAsync(h + 1, dv + o_cnt + 64, sizeof(int), cudaMemcpyDeviceToHost,
-                                     c->stream),
-                     "D2H lattice flag");
-  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "lattice kernel");
-  if (st) return st;
-  if (*(const int*)(h + 1)) return set_error(PCF_ETIMEOUT, "lattice grid barrier gave up");
-  *price = h[0];
-  return PCF_OK;
+    // Scratch: up | dn | A | B | counters (barrier, err) | out.
+    const size_t nodes = (size_t)N + 1;
+    const size_t o_up = 0, o_dn = o_up + 8 * nodes, o_A = o_dn + 8 * nodes, o_B = o_A + 8 * nodes;
+    const size_t o_cnt = (o_B + 8 * nodes + 255) & ~(size_t)255;
+    const size_t o_out = o_cnt + 256;
+    const size_t total = o_out + 256;
+    st = ctx_ensure(c, total, 16 * nodes + 64);
+    if (st) return st;
+    char* dv = (char*)c->d_buf;
+    double* h = (double*)c->h_buf;
+    // The reference's pow(u, i) and pow(d, n - i) (src/binom_vanilla_amer.cpp:28,32).
+    for (size_t i = 0; i < nodes; ++i) {
+      h[i] = pow(u, (double)i);
+      h[nodes + i] = pow(d, (double)i);
+    }
+    st = cuda_status(cudaMemcpyAsync(dv + o_up, h, 16 * nodes, cudaMemcpyHostToDevice, c->stream),
+                     "H2D lattice tables");
+    if (!st)
+      st = cuda_status(cudaMemsetAsync(dv + o_cnt, 0, 256, c->stream), "memset lattice counters");
+    if (st) return st;
+    LatticeParams P;
+    memset(&P, 0, sizeof P);
+    P.S0 = S0;
+    P.E = E;
+    P.p = p;
+    P.q = q;
+    P.R = R;
+    P.N = N;
+    P.pf = payoff_fun;
+    P.american = american ? 1 : 0;
+    P.up = (const double*)(dv + o_up);
+    P.dn = (const double*)(dv + o_dn);
+    P.A = (double*)(dv + o_A);
+    P.B = (double*)(dv + o_B);
+    P.barrier = (unsigned*)(dv + o_cnt);
+    P.err = (int*)(dv + o_cnt + 64);
+    P.wait_limit = 1u << 22;
+    if (c->test_barrier_extra) {  // test hook: a barrier that cannot complete
+      P.barrier_extra = c->test_barrier_extra;
+      P.wait_limit = c->test_poll_limit;
+    }
+    P.out = (double*)(dv + o_out);
+    int cap = seg_cap;
+    void* args[] = {&P, &cap};
+    st = cuda_status(cudaLaunchCooperativeKernel((void*)lattice_kernel, dim3(G), dim3(kLatBlock),
+                                                 args, smem, c->stream),
+                     "lattice kernel launch");
+    if (st) return st;
+    c->launches += 1;
+    st = cuda_status(cudaMemcpyAsync(h, dv + o_out, 8, cudaMemcpyDeviceToHost, c->stream),
+                     "D2H lattice");
+    if (!st)
+      st = cuda_status(cudaMemcpyAsync(h + 1, dv + o_cnt + 64, sizeof(int), cudaMemcpyDeviceToHost,
+                                       c->stream),
+                       "D2H lattice flag");
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "lattice kernel");
+    if (st) return st;
+    if (*(const int*)(h + 1)) return set_error(PCF_ETIMEOUT, "lattice grid barrier gave up");
+    *price = h[0];
+    return PCF_OK;
+  });
 }

@@ -1699,14 +1699,18 @@ int amer_run(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T
 extern "C" int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
                            long long N, int M, int payoff_fun, int ref_exercise,
                            unsigned long long seed, int use_cv, pcf_mc_result* out) {
-  return amer_run(ctx, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, use_cv, out,
-                  nullptr);
+  return pcf::abi_guard([&]() -> int {
+    return amer_run(ctx, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, use_cv, out,
+                    nullptr);
+  });
 }
 
 extern "C" int pcf_mc_amer_audit(pcf_ctx* ctx, double S0, double E, double r, double sigma,
                                  double T, long long N, int M, int payoff_fun, int ref_exercise,
                                  unsigned long long seed, pcf_mc_result* out, float* coef,
                                  double* sums, unsigned short* tau, float* u) {
-  const AmerAudit au{coef, sums, tau, u};
-  return amer_run(ctx, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, 1, out, &au);
+  return pcf::abi_guard([&]() -> int {
+    const AmerAudit au{coef, sums, tau, u};
+    return amer_run(ctx, S0, E, r, sigma, T, N, M, payoff_fun, ref_exercise, seed, 1, out, &au);
+  });
 }

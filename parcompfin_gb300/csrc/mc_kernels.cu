@@ -786,32 +786,34 @@ int noalloc_setup(unsigned char** addr, int dev) {
 extern "C" int pcf_mc_eur_noalloc(double S0, double E, double r, double sigma, double T,
                                   long long N, int payoff_fun, unsigned long long seed,
                                   double* d_sums, void* stream) {
-  using namespace pcf;
-  if (!d_sums) return set_error(PCF_EINVAL, "d_sums is NULL");
-  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
-  if (st) return st;
-  if (N > kNoAllocMaxPaths)
-    return set_error(PCF_EINVAL,
-                     "N = %lld exceeds the no-allocation limit of %lld paths (the fixed "
-                     "scratch holds %d work items)",
-                     N, (long long)kNoAllocMaxPaths, kNoAllocMaxItems);
-  int dev = 0;
-  st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
-  if (st) return st;
-  if (dev < 0 || dev >= kNoAllocMaxDevices)
-    return set_error(PCF_EINVAL, "device %d beyond the no-allocation table", dev);
-  unsigned char* scratch = nullptr;
-  st = noalloc_setup(&scratch, dev);
-  if (st) return st;
-  // The built-in work shape (256-thread items of at most 64 quads per
-  // thread), whatever a tuner chose: the scratch size above is derived from it.
-  const McContract C = make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0, TuneTable{});
-  if (C.items > kNoAllocMaxItems)
-    return set_error(PCF_EINVAL, "N = %lld needs %d work items; the fixed scratch holds %d", N,
-                     C.items, kNoAllocMaxItems);
-  cudaStream_t s = (cudaStream_t)stream;
-  st = cuda_status(cudaMemsetAsync(scratch, 0, sizeof(unsigned), s), "memset no-alloc ticket");
-  if (st) return st;
-  mc_eur_noalloc_kernel<<<C.items, kBlock, 0, s>>>(C, scratch, d_sums);
-  return cuda_status(cudaGetLastError(), "no-alloc kernel launch");
+  return pcf::abi_guard([&]() -> int {
+    using namespace pcf;
+    if (!d_sums) return set_error(PCF_EINVAL, "d_sums is NULL");
+    int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+    if (st) return st;
+    if (N > kNoAllocMaxPaths)
+      return set_error(PCF_EINVAL,
+                       "N = %lld exceeds the no-allocation limit of %lld paths (the fixed "
+                       "scratch holds %d work items)",
+                       N, (long long)kNoAllocMaxPaths, kNoAllocMaxItems);
+    int dev = 0;
+    st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st) return st;
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+      return set_error(PCF_EINVAL, "device %d beyond the no-allocation table", dev);
+    unsigned char* scratch = nullptr;
+    st = noalloc_setup(&scratch, dev);
+    if (st) return st;
+    // The built-in work shape (256-thread items of at most 64 quads per
+    // thread), whatever a tuner chose: the scratch size above is derived from it.
+    const McContract C = make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0, TuneTable{});
+    if (C.items > kNoAllocMaxItems)
+      return set_error(PCF_EINVAL, "N = %lld needs %d work items; the fixed scratch holds %d", N,
+                       C.items, kNoAllocMaxItems);
+    cudaStream_t s = (cudaStream_t)stream;
+    st = cuda_status(cudaMemsetAsync(scratch, 0, sizeof(unsigned), s), "memset no-alloc ticket");
+    if (st) return st;
+    mc_eur_noalloc_kernel<<<C.items, kBlock, 0, s>>>(C, scratch, d_sums);
+    return cuda_status(cudaGetLastError(), "no-alloc kernel launch");
+  });
 }

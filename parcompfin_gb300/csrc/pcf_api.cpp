@@ -14,16 +14,16 @@
 
 namespace pcf {
 
-static thread_local std::string g_err;
+static thread_local char g_err[512];  // the calling thread's last error (no allocation)
 static thread_local pcf_ctx* g_default_ctx = nullptr;
 
 int set_error(int status, const char* fmt, ...) {
-  char buf[512];
+  char buf[sizeof g_err];  // an argument may be the previous message itself
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  g_err = buf;
+  memcpy(g_err, buf, sizeof buf);
   return status;
 }
 
@@ -302,43 +302,47 @@ const char* pcf_strerror(int s) {
   return "unknown status";
 }
 
-const char* pcf_last_error(void) { return g_err.c_str(); }
+const char* pcf_last_error(void) { return g_err; }
 
 int pcf_ctx_create(int device, pcf_ctx** out) {
-  if (!out) return set_error(PCF_EINVAL, "out is NULL");
-  *out = nullptr;
-  int n = 0;
-  int st = cuda_status(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
-  if (st) return st;
-  if (device < 0 || device >= n)
-    return set_error(n == 0 ? PCF_ENODEV : PCF_EINVAL, "device %d not present (%d devices)",
-                     device, n);
-  st = cuda_status(cudaSetDevice(device), "cudaSetDevice");
-  if (st) return st;
-  pcf_ctx* c = new pcf_ctx();
-  c->device = device;
-  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
-  st = cuda_status(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
-  if (st) {
-    delete c;
-    return st;
-  }
-  *out = c;
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!out) return set_error(PCF_EINVAL, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    int st = cuda_status(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (st) return st;
+    if (device < 0 || device >= n)
+      return set_error(n == 0 ? PCF_ENODEV : PCF_EINVAL, "device %d not present (%d devices)",
+                       device, n);
+    st = cuda_status(cudaSetDevice(device), "cudaSetDevice");
+    if (st) return st;
+    pcf_ctx* c = new pcf_ctx();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    st = cuda_status(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+    if (st) {
+      delete c;
+      return st;
+    }
+    *out = c;
+    return PCF_OK;
+  });
 }
 
 int pcf_ctx_destroy(pcf_ctx* c) {
-  if (!c) return PCF_OK;
-  cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  serve_release(c);
-  ctx_release_extras(c);
-  if (c->d_buf) cudaFree(c->d_buf);
-  if (c->h_buf) cudaFreeHost(c->h_buf);
-  cudaStreamDestroy(c->stream);
-  if (c == g_default_ctx) g_default_ctx = nullptr;
-  delete c;
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!c) return PCF_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    serve_release(c);
+    ctx_release_extras(c);
+    if (c->d_buf) cudaFree(c->d_buf);
+    if (c->h_buf) cudaFreeHost(c->h_buf);
+    cudaStreamDestroy(c->stream);
+    if (c == g_default_ctx) g_default_ctx = nullptr;
+    delete c;
+    return PCF_OK;
+  });
 }
 
 void* pcf_ctx_stream(pcf_ctx* c) {
@@ -354,115 +358,129 @@ long long pcf_ctx_launch_count(pcf_ctx* c) {
 }
 
 int pcf_ctx_release(pcf_ctx* c) {
-  int st;
-  c = resolve_ctx(c, &st);
-  if (!c) return st;
-  cudaSetDevice(c->device);
-  st = cuda_status(cudaStreamSynchronize(c->stream), "context stream");
-  serve_release(c);
-  ctx_release_extras(c);
-  if (c->d_buf) cudaFree(c->d_buf);
-  if (c->h_buf) cudaFreeHost(c->h_buf);
-  c->d_buf = nullptr;
-  c->h_buf = nullptr;
-  c->d_cap = c->h_cap = 0;
-  return st;
+  return pcf::abi_guard([&]() -> int {
+    int st;
+    c = resolve_ctx(c, &st);
+    if (!c) return st;
+    cudaSetDevice(c->device);
+    st = cuda_status(cudaStreamSynchronize(c->stream), "context stream");
+    serve_release(c);
+    ctx_release_extras(c);
+    if (c->d_buf) cudaFree(c->d_buf);
+    if (c->h_buf) cudaFreeHost(c->h_buf);
+    c->d_buf = nullptr;
+    c->h_buf = nullptr;
+    c->d_cap = c->h_cap = 0;
+    return st;
+  });
 }
 
 int pcf_ctx_set_memory_limit(pcf_ctx* c, unsigned long long bytes) {
-  int st;
-  c = resolve_ctx(c, &st);
-  if (!c) return st;
-  c->budget_bytes = (size_t)bytes;
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    int st;
+    c = resolve_ctx(c, &st);
+    if (!c) return st;
+    c->budget_bytes = (size_t)bytes;
+    return PCF_OK;
+  });
 }
 
 int pcf_ctx_set_test_barrier(pcf_ctx* ctx, unsigned extra_arrivals, unsigned poll_limit) {
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  if (extra_arrivals && poll_limit < 1)
-    return set_error(PCF_EINVAL, "poll_limit must be >= 1 with extra arrivals");
-  c->test_barrier_extra = extra_arrivals;
-  c->test_poll_limit = extra_arrivals ? poll_limit : 0;
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    if (extra_arrivals && poll_limit < 1)
+      return set_error(PCF_EINVAL, "poll_limit must be >= 1 with extra arrivals");
+    c->test_barrier_extra = extra_arrivals;
+    c->test_poll_limit = extra_arrivals ? poll_limit : 0;
+    return PCF_OK;
+  });
 }
 
 int pcf_mc_eur(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T, long long N,
                int payoff_fun, unsigned long long seed, int use_cv, pcf_mc_result* out) {
-  if (!out) return set_error(PCF_EINVAL, "out is NULL");
-  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
-  if (st) return st;
-  if (N > (1LL << 46)) return set_error(PCF_EINVAL, "N must be <= 2^46");
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  const TuneTable tt = tune_table(c->device);
-  std::vector<McContract> cs{make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0, tt)};
-  std::vector<double> sums;
-  st = run_mc(c, MC_EUR, cs, {}, 0, tt.eur_block, false, false, use_cv != 0, sums);
-  if (st) return st;
-  fill_result(sums.data(), N, S0 * exp(r * T), exp(-r * T), use_cv != 0, out);
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!out) return set_error(PCF_EINVAL, "out is NULL");
+    int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+    if (st) return st;
+    if (N > (1LL << 46)) return set_error(PCF_EINVAL, "N must be <= 2^46");
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    const TuneTable tt = tune_table(c->device);
+    std::vector<McContract> cs{make_eur(S0, E, r, sigma, T, N, payoff_fun, seed, 0, tt)};
+    std::vector<double> sums;
+    st = run_mc(c, MC_EUR, cs, {}, 0, tt.eur_block, false, false, use_cv != 0, sums);
+    if (st) return st;
+    fill_result(sums.data(), N, S0 * exp(r * T), exp(-r * T), use_cv != 0, out);
+    return PCF_OK;
+  });
 }
 
 int pcf_mc_asia(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T, long long N,
                 int M, int payoff_fun, int mode, unsigned long long seed, int use_cv,
                 pcf_mc_result* out) {
-  if (!out) return set_error(PCF_EINVAL, "out is NULL");
-  int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
-  if (st) return st;
-  if (M < 1 || M > (1 << 20)) return set_error(PCF_EINVAL, "M must be in [1, 2^20]");
-  if (mode != 0 && mode != 1) return set_error(PCF_EINVAL, "mode must be 0 or 1");
-  if (N > (1LL << 38)) return set_error(PCF_EINVAL, "N must be <= 2^38");
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  const TuneTable tt = tune_table(c->device);
-  std::vector<McContract> cs{make_asia(S0, E, r, sigma, T, N, M, payoff_fun, mode, seed, 0, tt)};
-  std::vector<double> sums;
-  st = run_mc(c, MC_ASIA, cs, {}, 0, tt.asia_block, false, false, use_cv != 0, sums);
-  if (st) return st;
-  fill_result(sums.data(), N, asia_cv_mean(S0, E, r, sigma, T, M, payoff_fun, mode),
-              exp(-r * T), use_cv != 0, out);
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!out) return set_error(PCF_EINVAL, "out is NULL");
+    int st = check_common(S0, E, r, sigma, T, N, payoff_fun);
+    if (st) return st;
+    if (M < 1 || M > (1 << 20)) return set_error(PCF_EINVAL, "M must be in [1, 2^20]");
+    if (mode != 0 && mode != 1) return set_error(PCF_EINVAL, "mode must be 0 or 1");
+    if (N > (1LL << 38)) return set_error(PCF_EINVAL, "N must be <= 2^38");
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    const TuneTable tt = tune_table(c->device);
+    std::vector<McContract> cs{make_asia(S0, E, r, sigma, T, N, M, payoff_fun, mode, seed, 0, tt)};
+    std::vector<double> sums;
+    st = run_mc(c, MC_ASIA, cs, {}, 0, tt.asia_block, false, false, use_cv != 0, sums);
+    if (st) return st;
+    fill_result(sums.data(), N, asia_cv_mean(S0, E, r, sigma, T, M, payoff_fun, mode),
+                exp(-r * T), use_cv != 0, out);
+    return PCF_OK;
+  });
 }
 
 int pcf_mc_basket(pcf_ctx* ctx, int d, const double* S0, const double* sigma, const double* corr,
                   double r, double T, double E, long long N, int payoff_fun, int scale_by_sqrt_T,
                   unsigned long long seed, int use_cv, pcf_mc_result* out) {
-  if (!out || !S0 || !sigma || !corr) return set_error(PCF_EINVAL, "NULL pointer argument");
-  int st = check_common(1.0, E, r, 0.0, T, N, payoff_fun);
-  if (st) return st;
-  if (N > (1LL << 38)) return set_error(PCF_EINVAL, "N must be <= 2^38");
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  std::vector<float> fb;
-  McContract k;
-  double mu_g = 0;
-  const TuneTable tt = tune_table(c->device);
-  st = make_basket(d, S0, sigma, corr, r, T, E, N, payoff_fun, scale_by_sqrt_T ? sqrt(T) : 1.0,
-                   seed, 0, fb, k, mu_g, tt);
-  if (st) return st;
-  std::vector<McContract> cs{k};
-  std::vector<double> sums;
-  st = run_mc(c, MC_BASKET, cs, fb, d, mc_block(PCF_METHOD_BASKET, d, tt), basket_tensor(d, tt),
-              false, use_cv != 0, sums);
-  if (st) return st;
-  fill_result(sums.data(), N, mu_g, exp(-r * T), use_cv != 0, out);
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!out || !S0 || !sigma || !corr) return set_error(PCF_EINVAL, "NULL pointer argument");
+    int st = check_common(1.0, E, r, 0.0, T, N, payoff_fun);
+    if (st) return st;
+    if (N > (1LL << 38)) return set_error(PCF_EINVAL, "N must be <= 2^38");
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    std::vector<float> fb;
+    McContract k;
+    double mu_g = 0;
+    const TuneTable tt = tune_table(c->device);
+    st = make_basket(d, S0, sigma, corr, r, T, E, N, payoff_fun, scale_by_sqrt_T ? sqrt(T) : 1.0,
+                     seed, 0, fb, k, mu_g, tt);
+    if (st) return st;
+    std::vector<McContract> cs{k};
+    std::vector<double> sums;
+    st = run_mc(c, MC_BASKET, cs, fb, d, mc_block(PCF_METHOD_BASKET, d, tt), basket_tensor(d, tt),
+                false, use_cv != 0, sums);
+    if (st) return st;
+    fill_result(sums.data(), N, mu_g, exp(-r * T), use_cv != 0, out);
+    return PCF_OK;
+  });
 }
 
 int pcf_mc_eur_multi(pcf_ctx* ctx, double S0, double E, double r, double sigma, double T,
                      long long N, int payoff_fun, int assets, double rho,
                      unsigned long long seed, int use_cv, pcf_mc_result* out) {
-  if (assets < 1 || assets > 64) return set_error(PCF_EINVAL, "assets must be in [1, 64]");
-  if (!std::isfinite(rho) || rho < -1 || rho > 1)
-    return set_error(PCF_EINVAL, "rho must be in [-1, 1]");
-  // include/mvn.h:55-60: covariance with 1 on the diagonal and rho elsewhere.
-  std::vector<double> s0((size_t)assets, S0), sg((size_t)assets, sigma),
-      cor((size_t)assets * assets, rho);
-  for (int a = 0; a < assets; ++a) cor[(size_t)a * assets + a] = 1.0;
-  return pcf_mc_basket(ctx, assets, s0.data(), sg.data(), cor.data(), r, T, E, N, payoff_fun, 0,
-                       seed, use_cv, out);
+  return pcf::abi_guard([&]() -> int {
+    if (assets < 1 || assets > 64) return set_error(PCF_EINVAL, "assets must be in [1, 64]");
+    if (!std::isfinite(rho) || rho < -1 || rho > 1)
+      return set_error(PCF_EINVAL, "rho must be in [-1, 1]");
+    // include/mvn.h:55-60: covariance with 1 on the diagonal and rho elsewhere.
+    std::vector<double> s0((size_t)assets, S0), sg((size_t)assets, sigma),
+        cor((size_t)assets * assets, rho);
+    for (int a = 0; a < assets; ++a) cor[(size_t)a * assets + a] = 1.0;
+    return pcf_mc_basket(ctx, assets, s0.data(), sg.data(), cor.data(), r, T, E, N, payoff_fun, 0,
+                         seed, use_cv, out);
+  });
 }
 
 }  // extern "C"

@@ -6,6 +6,8 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <exception>
+#include <new>
 #include <vector>
 
 #include "../../include/pcf.h"
@@ -44,6 +46,22 @@ struct pcf_ctx {
 namespace pcf {
 
 int set_error(int status, const char* fmt, ...);
+
+// Runs the body of a C entry point and turns a C++ exception thrown inside it
+// (host memory exhausted in a std::vector, a failed thread start) into a
+// status with its message: no exception crosses the C ABI.
+template <class Body>
+int abi_guard(Body&& body) noexcept {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    return set_error(PCF_ENOMEM, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return set_error(PCF_EINVAL, "internal error: %s", e.what());
+  } catch (...) {
+    return set_error(PCF_EINVAL, "internal error");
+  }
+}
 int cuda_status(cudaError_t e, const char* what);
 int ctx_ensure(pcf_ctx* c, size_t dev_bytes, size_t host_bytes);
 pcf_ctx* resolve_ctx(pcf_ctx* ctx, int* status);

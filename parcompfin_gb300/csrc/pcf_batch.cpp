@@ -431,63 +431,75 @@ int plan_fill_results(pcf_plan* p, pcf_mc_result* results) {
 extern "C" {
 
 int pcf_plan_create(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_plan** out) {
-  if (!out || (n > 0 && !reqs) || n < 0) return set_error(PCF_EINVAL, "bad plan arguments");
-  *out = nullptr;
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  return plan_build(c, n, reqs, c->stream, nullptr, out);
+  return pcf::abi_guard([&]() -> int {
+    if (!out || (n > 0 && !reqs) || n < 0) return set_error(PCF_EINVAL, "bad plan arguments");
+    *out = nullptr;
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    return plan_build(c, n, reqs, c->stream, nullptr, out);
+  });
 }
 
 int pcf_plan_launch(pcf_plan* p) {
-  if (!p) return set_error(PCF_EINVAL, "plan is NULL");
-  cudaSetDevice(p->ctx->device);
-  return plan_launch(p);
+  return pcf::abi_guard([&]() -> int {
+    if (!p) return set_error(PCF_EINVAL, "plan is NULL");
+    cudaSetDevice(p->ctx->device);
+    return plan_launch(p);
+  });
 }
 
 int pcf_plan_set_graph(pcf_plan* p, int mode) {
-  if (!p || mode < 0 || mode > 1) return set_error(PCF_EINVAL, "bad arguments");
-  cudaSetDevice(p->ctx->device);
-  p->graph_mode = mode;
-  if (!mode && p->gexec) {
-    cudaStreamSynchronize(p->stream);
-    cudaGraphExecDestroy(p->gexec);
-    p->gexec = nullptr;
-  }
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!p || mode < 0 || mode > 1) return set_error(PCF_EINVAL, "bad arguments");
+    cudaSetDevice(p->ctx->device);
+    p->graph_mode = mode;
+    if (!mode && p->gexec) {
+      cudaStreamSynchronize(p->stream);
+      cudaGraphExecDestroy(p->gexec);
+      p->gexec = nullptr;
+    }
+    return PCF_OK;
+  });
 }
 
 int pcf_plan_uses_graph(const pcf_plan* p) { return p && p->gexec ? 1 : 0; }
 
 int pcf_plan_kernel_count(const pcf_plan* p) {
-  return p ? (int)p->groups.size() + (p->lsm ? lsm_batch_kernels(p->lsm) : 0) : 0;
+  return pcf::abi_guard([&]() -> int {
+    return p ? (int)p->groups.size() + (p->lsm ? lsm_batch_kernels(p->lsm) : 0) : 0;
+  });
 }
 
 int pcf_plan_results(pcf_plan* p, pcf_mc_result* results) {
-  if (!p || (p->n && !results)) return set_error(PCF_EINVAL, "bad arguments");
-  cudaSetDevice(p->ctx->device);
-  int st = plan_fetch(p);
-  if (!st) st = cuda_status(cudaStreamSynchronize(p->stream), "batch kernels");
-  if (st) return st;
-  return plan_fill_results(p, results);
+  return pcf::abi_guard([&]() -> int {
+    if (!p || (p->n && !results)) return set_error(PCF_EINVAL, "bad arguments");
+    cudaSetDevice(p->ctx->device);
+    int st = plan_fetch(p);
+    if (!st) st = cuda_status(cudaStreamSynchronize(p->stream), "batch kernels");
+    if (st) return st;
+    return plan_fill_results(p, results);
+  });
 }
 
 int pcf_plan_destroy(pcf_plan* p) {
-  if (!p) return PCF_OK;
-  cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->stream);
-  if (p->gexec) cudaGraphExecDestroy(p->gexec);
-  if (p->side) {
-    cudaStreamSynchronize(p->side);
-    cudaStreamDestroy(p->side);
-  }
-  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
-  if (p->ev_join) cudaEventDestroy(p->ev_join);
-  lsm_batch_destroy(p->lsm);
-  if (p->d_mem) cudaFree(p->d_mem);
-  if (p->h_own) cudaFreeHost(p->h_own);
-  delete p;
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!p) return PCF_OK;
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->stream);
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->side) {
+      cudaStreamSynchronize(p->side);
+      cudaStreamDestroy(p->side);
+    }
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
+    lsm_batch_destroy(p->lsm);
+    if (p->d_mem) cudaFree(p->d_mem);
+    if (p->h_own) cudaFreeHost(p->h_own);
+    delete p;
+    return PCF_OK;
+  });
 }
 
 // The one-shot plan lives in the context's scratch arena (device and pinned
@@ -496,37 +508,39 @@ int pcf_plan_destroy(pcf_plan* p) {
 // reports how far the arena must reach; the arena grows and the build runs
 // again (at most a few times, only while the arena grows).
 int pcf_price_batch(pcf_ctx* ctx, int n, const pcf_mc_request* reqs, pcf_mc_result* results) {
-  if (n < 0 || (n > 0 && (!reqs || !results))) return set_error(PCF_EINVAL, "bad batch arguments");
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  cudaSetDevice(c->device);
-  size_t dneed = std::max(c->d_cap, (size_t)1 << 20), hneed = std::max(c->h_cap, (size_t)1 << 20);
-  pcf_plan* p = nullptr;
-  for (int attempt = 0;; ++attempt) {
-    st = ctx_ensure(c, dneed, hneed);
+  return pcf::abi_guard([&]() -> int {
+    if (n < 0 || (n > 0 && (!reqs || !results))) return set_error(PCF_EINVAL, "bad batch arguments");
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    cudaSetDevice(c->device);
+    size_t dneed = std::max(c->d_cap, (size_t)1 << 20), hneed = std::max(c->h_cap, (size_t)1 << 20);
+    pcf_plan* p = nullptr;
+    for (int attempt = 0;; ++attempt) {
+      st = ctx_ensure(c, dneed, hneed);
+      if (st) return st;
+      ExtMem mem;
+      mem.d = (char*)c->d_buf;
+      mem.d_cap = c->d_cap;
+      mem.h = (char*)c->h_buf;
+      mem.h_cap = c->h_cap;
+      st = plan_build(c, n, reqs, c->stream, &mem, &p);
+      if (st != PCF_ENOMEM || (!mem.d_short && !mem.h_short) || attempt == 4) break;
+      // Grow past the shortfall; later parts of the build may need more. A
+      // failed build may have queued its table upload: let it land before the
+      // arena is replaced.
+      cudaStreamSynchronize(c->stream);
+      dneed = std::max(dneed, mem.d_short + mem.d_short / 4);
+      hneed = std::max(hneed, mem.h_short + mem.h_short / 4);
+    }
     if (st) return st;
-    ExtMem mem;
-    mem.d = (char*)c->d_buf;
-    mem.d_cap = c->d_cap;
-    mem.h = (char*)c->h_buf;
-    mem.h_cap = c->h_cap;
-    st = plan_build(c, n, reqs, c->stream, &mem, &p);
-    if (st != PCF_ENOMEM || (!mem.d_short && !mem.h_short) || attempt == 4) break;
-    // Grow past the shortfall; later parts of the build may need more. A
-    // failed build may have queued its table upload: let it land before the
-    // arena is replaced.
-    cudaStreamSynchronize(c->stream);
-    dneed = std::max(dneed, mem.d_short + mem.d_short / 4);
-    hneed = std::max(hneed, mem.h_short + mem.h_short / 4);
-  }
-  if (st) return st;
-  st = plan_launch(p);
-  if (!st) st = plan_fetch(p);
-  if (!st) st = cuda_status(cudaStreamSynchronize(p->stream), "batch kernels");
-  if (!st) st = plan_fill_results(p, results);
-  pcf_plan_destroy(p);
-  return st;
+    st = plan_launch(p);
+    if (!st) st = plan_fetch(p);
+    if (!st) st = cuda_status(cudaStreamSynchronize(p->stream), "batch kernels");
+    if (!st) st = plan_fill_results(p, results);
+    pcf_plan_destroy(p);
+    return st;
+  });
 }
 
 }  // extern "C"

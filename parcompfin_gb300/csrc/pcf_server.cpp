@@ -492,46 +492,48 @@ void fill_stats(const pcf_served_result* out, int n, double first_arrival, int b
 extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, int n,
                                const pcf_mc_request* reqs, const double* arrival,
                                pcf_served_result* out, pcf_server_stats* stats) {
-  if (n < 0 || (n > 0 && (!reqs || !arrival || !out))) return set_error(PCF_EINVAL, "bad arguments");
-  pcf_server_config cfg = cfg_in ? *cfg_in : pcf_server_config{};
-  fill_defaults(cfg);
-  for (int i = 1; i < n; ++i)
-    if (arrival[i] < arrival[i - 1]) return set_error(PCF_EINVAL, "arrival times must not decrease");
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  ServeCache* sc = nullptr;
-  st = reserve_slots(c, cfg, &sc);
-  if (st) return st;
-  for (int i = 0; i < n; ++i) {
-    memset(&out[i], 0, sizeof out[i]);
-    out[i].arrival_s = arrival[i];
-    out[i].status = PCF_OK;
-  }
-  ServeLoop loop(c, cfg, sc, Clock::now(),
-                 [out](int id, const pcf_served_result& r) { out[id] = r; });
-  int next = 0;
-  while (loop.done < n) {
-    const double t = loop.now();
-    while (next < n && arrival[next] <= t) {
-      loop.admit(next, reqs[next], arrival[next]);
-      ++next;
+  return pcf::abi_guard([&]() -> int {
+    if (n < 0 || (n > 0 && (!reqs || !arrival || !out))) return set_error(PCF_EINVAL, "bad arguments");
+    pcf_server_config cfg = cfg_in ? *cfg_in : pcf_server_config{};
+    fill_defaults(cfg);
+    for (int i = 1; i < n; ++i)
+      if (arrival[i] < arrival[i - 1]) return set_error(PCF_EINVAL, "arrival times must not decrease");
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    ServeCache* sc = nullptr;
+    st = reserve_slots(c, cfg, &sc);
+    if (st) return st;
+    for (int i = 0; i < n; ++i) {
+      memset(&out[i], 0, sizeof out[i]);
+      out[i].arrival_s = arrival[i];
+      out[i].status = PCF_OK;
     }
-    if (!loop.pass()) {
-      if (next < n && loop.idle()) {
-        // Nothing to do until the next arrival.
-        if (arrival[next] - loop.now() > 200e-6)
-          std::this_thread::sleep_for(std::chrono::microseconds(50));
-      } else {
-        std::this_thread::sleep_for(std::chrono::microseconds(10));
+    ServeLoop loop(c, cfg, sc, Clock::now(),
+                   [out](int id, const pcf_served_result& r) { out[id] = r; });
+    int next = 0;
+    while (loop.done < n) {
+      const double t = loop.now();
+      while (next < n && arrival[next] <= t) {
+        loop.admit(next, reqs[next], arrival[next]);
+        ++next;
+      }
+      if (!loop.pass()) {
+        if (next < n && loop.idle()) {
+          // Nothing to do until the next arrival.
+          if (arrival[next] - loop.now() > 200e-6)
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        } else {
+          std::this_thread::sleep_for(std::chrono::microseconds(10));
+        }
       }
     }
-  }
-  loop.release();
-  if (stats)
-    fill_stats(out, n, n ? arrival[0] : 0.0, loop.batches, loop.paths,
-               sc->per_slot * sc->slots.size(), stats);
-  return loop.failures ? loop.first_error : PCF_OK;
+    loop.release();
+    if (stats)
+      fill_stats(out, n, n ? arrival[0] : 0.0, loop.batches, loop.paths,
+                 sc->per_slot * sc->slots.size(), stats);
+    return loop.failures ? loop.first_error : PCF_OK;
+  });
 }
 
 // ---- the live server -------------------------------------------------------
@@ -544,6 +546,8 @@ struct pcf_server {
   std::mutex mu;
   std::condition_variable work_cv;  // the worker: new requests or stop
   std::condition_variable done_cv;  // waiters: a request finished
+  std::condition_variable idle_cv;  // pcf_server_stop: no submit/poll/wait call in progress
+  int callers = 0;                  // submit/poll/wait calls in progress
   std::vector<pcf_mc_request> incoming;  // submitted, not yet taken by the worker
   long long first_incoming = 0;          // ticket of incoming[0]
   std::deque<pcf_served_result> out;     // by ticket
@@ -613,90 +617,131 @@ void serve_worker(pcf_server* s) {
 
 extern "C" int pcf_server_start(pcf_ctx* ctx, const pcf_server_config* cfg_in,
                                 pcf_server** out) {
-  if (!out) return set_error(PCF_EINVAL, "out is NULL");
-  *out = nullptr;
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  pcf_server* s = new pcf_server();
-  s->c = c;
-  s->cfg = cfg_in ? *cfg_in : pcf_server_config{};
-  fill_defaults(s->cfg);
-  st = reserve_slots(c, s->cfg, &s->sc);
-  if (st) {
-    delete s;
-    return st;
-  }
-  s->t0 = Clock::now();
-  try {
-    s->worker = std::thread(serve_worker, s);
-  } catch (const std::exception& e) {  // no C++ exception crosses the ABI
-    delete s;
-    return set_error(PCF_EINVAL, "cannot start the server's worker thread: %s", e.what());
-  }
-  *out = s;
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!out) return set_error(PCF_EINVAL, "out is NULL");
+    *out = nullptr;
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    pcf_server* s = new pcf_server();
+    s->c = c;
+    s->cfg = cfg_in ? *cfg_in : pcf_server_config{};
+    fill_defaults(s->cfg);
+    st = reserve_slots(c, s->cfg, &s->sc);
+    if (st) {
+      delete s;
+      return st;
+    }
+    s->t0 = Clock::now();
+    try {
+      s->worker = std::thread(serve_worker, s);
+    } catch (const std::exception& e) {  // no C++ exception crosses the ABI
+      delete s;
+      return set_error(PCF_EINVAL, "cannot start the server's worker thread: %s", e.what());
+    }
+    *out = s;
+    return PCF_OK;
+  });
 }
 
+namespace {
+
+// Counts a submit/poll/wait call in progress (under the server's mutex, held
+// by the caller for the guard's lifetime or reacquired by a condition-variable
+// wait before it ends), so that pcf_server_stop frees the server only after
+// every such call has returned.
+struct CallGuard {
+  pcf_server* s;
+  explicit CallGuard(pcf_server* srv) : s(srv) { ++s->callers; }
+  ~CallGuard() {
+    if (--s->callers == 0) s->idle_cv.notify_all();
+  }
+};
+
+}  // namespace
+
 extern "C" int pcf_server_submit(pcf_server* s, const pcf_mc_request* req, long long* ticket) {
-  if (!s || !req || !ticket) return set_error(PCF_EINVAL, "bad arguments");
-  std::lock_guard<std::mutex> lk(s->mu);
-  if (s->stop) return set_error(PCF_EINVAL, "the server is stopping");
-  const long long id = s->submitted++;
-  if (id > 0x7ffffff0LL) return set_error(PCF_EINVAL, "too many requests for one server");
-  pcf_served_result r;
-  memset(&r, 0, sizeof r);
-  r.arrival_s = std::chrono::duration<double>(Clock::now() - s->t0).count();
-  r.status = PCF_OK;
-  s->out.push_back(r);
-  s->finished.push_back(0);
-  s->incoming.push_back(*req);
-  *ticket = id;
-  s->work_cv.notify_one();
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!s || !req || !ticket) return set_error(PCF_EINVAL, "bad arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CallGuard guard(s);
+    if (s->stop) return set_error(PCF_EINVAL, "the server is stopping");
+    if (s->submitted > 0x7ffffff0LL) return set_error(PCF_EINVAL, "too many requests for one server");
+    pcf_served_result r;
+    memset(&r, 0, sizeof r);
+    r.arrival_s = std::chrono::duration<double>(Clock::now() - s->t0).count();
+    r.status = PCF_OK;
+    try {  // no C++ exception crosses the ABI; on failure nothing is queued
+      s->out.push_back(r);
+      s->finished.push_back(0);
+      s->incoming.push_back(*req);
+    } catch (const std::exception&) {
+      s->out.resize((size_t)s->submitted);
+      s->finished.resize((size_t)s->submitted);
+      return set_error(PCF_ENOMEM, "cannot queue the request");
+    }
+    *ticket = s->submitted++;
+    s->work_cv.notify_one();
+    return PCF_OK;
+  });
 }
 
 extern "C" int pcf_server_poll(pcf_server* s, long long ticket, pcf_served_result* out) {
-  if (!s || !out) return set_error(PCF_EINVAL, "bad arguments");
-  std::lock_guard<std::mutex> lk(s->mu);
-  if (ticket < 0 || ticket >= s->submitted) return set_error(PCF_EINVAL, "unknown ticket");
-  if (!s->finished[(size_t)ticket]) return PCF_PENDING;
-  *out = s->out[(size_t)ticket];
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!s || !out) return set_error(PCF_EINVAL, "bad arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CallGuard guard(s);
+    if (ticket < 0 || ticket >= s->submitted) return set_error(PCF_EINVAL, "unknown ticket");
+    if (!s->finished[(size_t)ticket]) return PCF_PENDING;
+    *out = s->out[(size_t)ticket];
+    return PCF_OK;
+  });
 }
 
 extern "C" int pcf_server_wait(pcf_server* s, long long ticket, double timeout_s,
                                pcf_served_result* out) {
-  if (!s || !out) return set_error(PCF_EINVAL, "bad arguments");
-  std::unique_lock<std::mutex> lk(s->mu);
-  if (ticket < 0 || ticket >= s->submitted) return set_error(PCF_EINVAL, "unknown ticket");
-  const auto ready = [&] { return s->finished[(size_t)ticket] != 0; };
-  if (timeout_s < 0) {
-    s->done_cv.wait(lk, ready);
-  } else if (!s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
-    return PCF_PENDING;
-  }
-  *out = s->out[(size_t)ticket];
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    if (!s || !out) return set_error(PCF_EINVAL, "bad arguments");
+    std::unique_lock<std::mutex> lk(s->mu);
+    CallGuard guard(s);
+    if (ticket < 0 || ticket >= s->submitted) return set_error(PCF_EINVAL, "unknown ticket");
+    const auto ready = [&] { return s->finished[(size_t)ticket] != 0; };
+    if (timeout_s < 0) {
+      s->done_cv.wait(lk, ready);
+    } else if (!s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
+      return PCF_PENDING;
+    }
+    *out = s->out[(size_t)ticket];
+    return PCF_OK;
+  });
 }
 
 extern "C" int pcf_server_stop(pcf_server* s, pcf_server_stats* stats) {
-  if (!s) return PCF_OK;
-  {
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->stop = true;
-  }
-  s->work_cv.notify_all();
-  if (s->worker.joinable()) s->worker.join();
-  int st = s->failures ? s->first_error : PCF_OK;
-  if (stats) {
-    std::vector<pcf_served_result> v(s->out.begin(), s->out.end());
-    double first = v.empty() ? 0.0 : v[0].arrival_s;
-    fill_stats(v.data(), (int)v.size(), first, s->batches, s->paths,
-               s->sc->per_slot * s->sc->slots.size(), stats);
-  }
-  delete s;
-  return st;
+  return pcf::abi_guard([&]() -> int {
+    if (!s) return PCF_OK;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stop = true;
+    }
+    s->work_cv.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    {
+      // Every request is finished now, so waiters wake; the server is freed
+      // only after the last call in progress has returned.
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->done_cv.notify_all();
+      s->idle_cv.wait(lk, [s] { return s->callers == 0; });
+    }
+    int st = s->failures ? s->first_error : PCF_OK;
+    if (stats) {
+      std::vector<pcf_served_result> v(s->out.begin(), s->out.end());
+      double first = v.empty() ? 0.0 : v[0].arrival_s;
+      fill_stats(v.data(), (int)v.size(), first, s->batches, s->paths,
+                 s->sc->per_slot * s->sc->slots.size(), stats);
+    }
+    delete s;
+    return st;
+  });
 }
 
 namespace pcf {

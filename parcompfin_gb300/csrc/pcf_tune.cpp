@@ -515,36 +515,44 @@ int run_tuner(pcf_ctx* c, int flags, const pcf_mc_request* ureqs, int un, char* 
 }  // namespace
 
 extern "C" int pcf_autotune(pcf_ctx* ctx, int flags, char* report, int report_len) {
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  return run_tuner(c, flags, nullptr, 0, report, report_len);
+  return pcf::abi_guard([&]() -> int {
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    return run_tuner(c, flags, nullptr, 0, report, report_len);
+  });
 }
 
 extern "C" int pcf_autotune_batch(pcf_ctx* ctx, int flags, int n, const pcf_mc_request* reqs,
                                   char* report, int report_len) {
-  if (n <= 0 || !reqs) return set_error(PCF_EINVAL, "the tuning batch is empty");
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  return run_tuner(c, flags, reqs, n, report, report_len);
+  return pcf::abi_guard([&]() -> int {
+    if (n <= 0 || !reqs) return set_error(PCF_EINVAL, "the tuning batch is empty");
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    return run_tuner(c, flags, reqs, n, report, report_len);
+  });
 }
 
 extern "C" int pcf_tune_report(pcf_ctx* ctx, char* report, int report_len) {
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  if (!report || report_len <= 0) return set_error(PCF_EINVAL, "report buffer is empty");
-  const std::string r = "{\"device\": \"" + device_name(c->device) + "\", \"table\": " +
-                        tune_json(tune_table(c->device)) + "}";
-  snprintf(report, (size_t)report_len, "%s", r.c_str());
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    if (!report || report_len <= 0) return set_error(PCF_EINVAL, "report buffer is empty");
+    const std::string r = "{\"device\": \"" + device_name(c->device) + "\", \"table\": " +
+                          tune_json(tune_table(c->device)) + "}";
+    snprintf(report, (size_t)report_len, "%s", r.c_str());
+    return PCF_OK;
+  });
 }
 
 extern "C" int pcf_tune_reset(pcf_ctx* ctx) {
-  int st;
-  pcf_ctx* c = resolve_ctx(ctx, &st);
-  if (!c) return st;
-  tune_reset(c->device);
-  return PCF_OK;
+  return pcf::abi_guard([&]() -> int {
+    int st;
+    pcf_ctx* c = resolve_ctx(ctx, &st);
+    if (!c) return st;
+    tune_reset(c->device);
+    return PCF_OK;
+  });
 }

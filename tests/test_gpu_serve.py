@@ -230,6 +230,44 @@ def test_live_server_admits_while_running_and_matches_alone(ctx):
     assert continued > 0
 
 
+def test_stop_while_other_threads_wait(ctx):
+    """pcf_server_stop called while other threads are blocked in
+    pcf_server_wait: stop drains every request, the waiters return with
+    their results, and the server is freed only after they have returned."""
+    import threading
+    import time
+
+    import parcompfin_gb300 as pcf
+    reqs = [pcf.request("amer", 100.0, 100.0 + k % 7, .05, .3, 1.0, 1 << 20, "put", M=50,
+                        seed=3, stream=k) for k in range(24)]
+    reqs += [pcf.request("eur", 100.0, 100.0, .05, .2, 1.0, 1 << 22, "call", seed=3, stream=100 + k)
+             for k in range(16)]
+    srv = pcf.Server(ctx, target_rel_se=0.0)
+    tickets = [srv.submit(q) for q in reqs]
+    got = {}
+    ready = threading.Barrier(4)
+
+    def waiter(t):  # one call each: no call may start once stop has returned
+        ready.wait()
+        got[t] = srv.wait(t, -1.0)
+
+    watched = [tickets[23], tickets[-2], tickets[-1]]
+    th = [threading.Thread(target=waiter, args=(t,)) for t in watched]
+    for t in th:
+        t.start()
+    ready.wait()
+    time.sleep(0.05)  # the waiters are inside pcf_server_wait by now
+    stats = srv.stop()
+    for t in th:
+        t.join(60)
+        assert not t.is_alive()
+    assert stats.completed == len(reqs)
+    assert sorted(got) == sorted(watched)
+    for t in watched:
+        assert got[t].status == 0 and got[t].result.n_paths == reqs[t]["N"]
+        assert math.isfinite(got[t].result.price) and got[t].result.price > 0
+
+
 def test_empty_inputs(ctx):
     """An empty trace, and a live server that serves nothing, finish with
     nothing completed; an empty batch prices nothing."""
