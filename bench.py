@@ -92,6 +92,11 @@ def _fp32_roofline(flop_per_unit, units, ms, sms, sm_mhz):
 # 1635.3 MB for 1677.7 MB algorithmic). Traffic grows with the path-dates, so
 # other launches of the kernel scale by it.
 LSM_TRAFFIC_PER_ALG_BYTE = 1635.3 / 1677.7
+# What bounds the American cluster kernel, from the same capture.
+LSM_LIMITER = ("the per-date regression chain, not HBM: each date is a fused pass over the "
+               "CTA's paths, then one warp reduces, exchanges the sums across the cluster and "
+               "solves while the other warps wait (ncu, 64-put launch: 58 % of issue slots "
+               "busy, DRAM 32 % of peak, barrier the top stall)")
 
 
 class EurWorkload:
@@ -373,6 +378,10 @@ class LsmWorkload:
         peak = peaks.get("hbm_gbs", 6800.0)
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                 "frac": ach / peak, "traffic": None,
+                "limiter": "the per-date chain of one contract spread over every SM: each of "
+                           "the 49 dates ends with an exchange of the regression sums across "
+                           "the whole grid (clusters, then their leaders in global memory) "
+                           "before the next date can start",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
                                "fallback 6.8 TB/s"}
 
@@ -657,6 +666,7 @@ class MixedWorkload:
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": alg * LSM_TRAFFIC_PER_ALG_BYTE,
                 "traffic_source": "ncu capture of the 64-put batch, scaled by path-dates",
+                "limiter": LSM_LIMITER,
                 "kernel_ms": t,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
                                "fallback 6.8 TB/s",
@@ -850,6 +860,7 @@ class AmerBatchWorkload:
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": alg * LSM_TRAFFIC_PER_ALG_BYTE,
                 "traffic_source": "ncu capture of this launch (dram bytes read + written)",
+                "limiter": LSM_LIMITER,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
 
     def cpu_reference(self, threads, budget_s):

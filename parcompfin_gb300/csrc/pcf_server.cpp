@@ -194,6 +194,9 @@ class ServeLoop {
   }
 
   // Leaves every slot free (a failed batch may hold a plan).
+  // Also run on unwinding, so an exception leaves no plan in a slot.
+  ~ServeLoop() { release(); }
+
   void release() {
     for (Slot& s : slots_) {
       if (s.plan) {
@@ -556,12 +559,13 @@ struct pcf_server {
   int batches = 0, failures = 0, first_error = PCF_OK;
   long long paths = 0;
   bool stop = false;
+  bool dead = false;  // the worker ended on an exception; submissions are refused
   std::thread worker;
 };
 
 namespace {
 
-void serve_worker(pcf_server* s) {
+void serve_worker_loop(pcf_server* s) {
   cudaSetDevice(s->c->device);
   ServeLoop loop(s->c, s->cfg, s->sc, s->t0, [s](int id, const pcf_served_result& r) {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -611,6 +615,30 @@ void serve_worker(pcf_server* s) {
     }
   }
   loop.release();
+}
+
+// The worker thread: a C++ exception in the loop (host memory exhausted)
+// would end the process from a thread, so it ends the server instead: every
+// request not yet finished gets the error as its status, so that no waiter
+// blocks for ever, and later submissions are refused.
+void serve_worker(pcf_server* s) {
+  try {
+    serve_worker_loop(s);
+  } catch (...) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->dead = true;
+    s->failures += 1;
+    if (s->first_error == PCF_OK) s->first_error = PCF_ENOMEM;
+    for (size_t i = 0; i < s->finished.size(); ++i)
+      if (!s->finished[i]) {
+        s->out[i].status = PCF_ENOMEM;
+        s->finished[i] = 1;
+        ++s->completed;
+      }
+    s->incoming.clear();
+    s->first_incoming = s->submitted;
+    s->done_cv.notify_all();
+  }
 }
 
 }  // namespace
@@ -666,6 +694,7 @@ extern "C" int pcf_server_submit(pcf_server* s, const pcf_mc_request* req, long 
     std::lock_guard<std::mutex> lk(s->mu);
     CallGuard guard(s);
     if (s->stop) return set_error(PCF_EINVAL, "the server is stopping");
+    if (s->dead) return set_error(PCF_ENOMEM, "the server's worker ended on an error");
     if (s->submitted > 0x7ffffff0LL) return set_error(PCF_EINVAL, "too many requests for one server");
     pcf_served_result r;
     memset(&r, 0, sizeof r);
