@@ -54,6 +54,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -638,48 +639,71 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
     float acc[kRegSums];
 #pragma unroll
     for (int q = 0; q < kRegSums; ++q) acc[q] = 0.f;
-    // Exercise decision at date m (src/mc_amer.cpp:73-106) for one path:
-    // exercise where the path is in the money and the payoff beats the
-    // continuation value; the cash flow becomes the payoff discounted to 0.
     const float E = P.E, nK = P.nK;
-    const bool refx = P.ref_exercise != 0;
-    auto decide = [&](float u, float& cfd, int s) {
-      float cont, ex = u * E;  // the payoff before its max with 0
-      if (mode == 1) {
-        cont = cfd * em;
-      } else {
-        cont = fmaf(fmaf(c2, u, c1), u, c0);
-        // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E),
-        // max(pf (S - 2E), 0) = max(E u - pf E, 0).
-        if (refx) ex = fmaxf(fmaf(E, u, nK), 0.f);
-      }
-      if (u > 0.f && ex > cont) {
-        cfd = ex * dm;
-        S.tau[s] = (TauT)m;
+    // One pass over the block's paths, compiled once per case (the date's
+    // mode MD, the reference's exercise rule RX, a following date NX), so
+    // the loop carries no per-path test of them.
+    auto sweep = [&](auto md_c, auto rx_c, auto nx_c) {
+      constexpr int MD = decltype(md_c)::value;
+      constexpr bool RX = decltype(rx_c)::value;
+      constexpr bool NX = decltype(nx_c)::value;
+      // Exercise decision at date m (src/mc_amer.cpp:73-106) for one path:
+      // exercise where the path is in the money and the payoff beats the
+      // continuation value; the cash flow becomes the payoff discounted to 0.
+      auto decide = [&](float u, float& cfd, int s) {
+        float cont, ex = u * E;  // the payoff before its max with 0
+        if (MD == 1) {
+          cont = cfd * em;
+        } else {
+          cont = fmaf(fmaf(c2, u, c1), u, c0);
+          // src/mc_amer.cpp:100: the reference exercises at payoff(S - E, E),
+          // max(pf (S - 2E), 0) = max(E u - pf E, 0).
+          if (RX) ex = fmaxf(fmaf(E, u, nK), 0.f);
+        }
+        if (u > 0.f && ex > cont) {
+          cfd = ex * dm;
+          S.tau[s] = (TauT)m;
+        }
+      };
+#pragma unroll 2
+      for (int j = threadIdx.x; j < nq; j += BS) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int s = h * PB + 4 * j;
+          float4 c = ld4(S.cf + s);
+          if (MD != 0) {
+            const float4 u = ld4(cur + s);
+            decide(u.x, c.x, s);
+            decide(u.y, c.y, s + 1);
+            decide(u.z, c.z, s + 2);
+            decide(u.w, c.w, s + 3);
+            st4(S.cf + s, c);
+          }
+          if (NX) {
+            const float4 u = ld4(nxt + s);
+            reg_accumulate(u.x, c.x, acc);
+            reg_accumulate(u.y, c.y, acc);
+            reg_accumulate(u.z, c.z, acc);
+            reg_accumulate(u.w, c.w, acc);
+          }
+        }
       }
     };
-#pragma unroll 2
-    for (int j = threadIdx.x; j < nq; j += BS) {
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int s = h * PB + 4 * j;
-        float4 c = ld4(S.cf + s);
-        if (mode != 0) {
-          const float4 u = ld4(cur + s);
-          decide(u.x, c.x, s);
-          decide(u.y, c.y, s + 1);
-          decide(u.z, c.z, s + 2);
-          decide(u.w, c.w, s + 3);
-          st4(S.cf + s, c);
-        }
-        if (has_next) {
-          const float4 u = ld4(nxt + s);
-          reg_accumulate(u.x, c.x, acc);
-          reg_accumulate(u.y, c.y, acc);
-          reg_accumulate(u.z, c.z, acc);
-          reg_accumulate(u.w, c.w, acc);
-        }
-      }
+    using Md0 = std::integral_constant<int, 0>;
+    using Md1 = std::integral_constant<int, 1>;
+    using Md2 = std::integral_constant<int, 2>;
+    using Yes = std::true_type;
+    using No = std::false_type;
+    const bool refx = P.ref_exercise != 0;
+    if (has_next) {
+      if (mode == 0) sweep(Md0{}, No{}, Yes{});
+      else if (mode == 1) sweep(Md1{}, No{}, Yes{});
+      else if (refx) sweep(Md2{}, Yes{}, Yes{});
+      else sweep(Md2{}, No{}, Yes{});
+    } else {
+      if (mode == 1) sweep(Md1{}, No{}, No{});
+      else if (mode == 2 && refx) sweep(Md2{}, Yes{}, No{});
+      else if (mode == 2) sweep(Md2{}, No{}, No{});
     }
     if (!has_next) break;
     regress(acc, m - 1, m - 2 >= 1 ? m - 3 : -1, k);
