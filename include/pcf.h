@@ -157,7 +157,8 @@ PCF_API int pcf_mc_amer(pcf_ctx* ctx, double S0, double E, double r, double sigm
  *              discounted to date d;
  *   tau[N]     each path's exercise date (M: held to T); paths p and
  *              p + N/2 are antithetic;
- *   u[M*N]     the FP32 path matrix: row m-1 holds u at date m.
+ *   u[M*N]     the FP32 path matrix: row m-1 holds max(u, 0) at date m
+ *              (only paths in the money, u > 0, enter the sweep).
  * Has no counterpart in the reference. */
 PCF_API int pcf_mc_amer_audit(pcf_ctx* ctx, double S0, double E, double r, double sigma,
                               double T, long long N, int M, int payoff_fun, int ref_exercise,

@@ -920,7 +920,8 @@ ORC_EXPORT void twin_mc_amer_audit(double S0, double E, double r, double sigma, 
   double du = 0;
 #pragma omp parallel for reduction(max : du) schedule(static)
   for (int64_t n = 0; n < N; ++n)
-    for (int m = 1; m <= M; ++m) du = std::max(du, fabs((double)U(m, n) - U64(m, n)));
+    for (int m = 1; m <= M; ++m)  /* the path matrix holds max(u, 0) */
+      du = std::max(du, fabs((double)U(m, n) - std::max(U64(m, n), 0.0)));
   rep[9] = du;
   std::vector<double> disc((size_t)M + 1);
   for (int k = 0; k <= M; ++k) disc[k] = exp(-r * dtd * k);
@@ -1223,8 +1224,8 @@ ORC_EXPORT void orc_emulate_lsm_record(double S0, double E, double r, double sig
       const double zm = z[(m - 1) % 4];
       lp += nu_dt + sigma * sdt * zm;
       lm += nu_dt - sigma * sdt * zm;
-      gu[(size_t)(m - 1) * N + p] = (float)(pf * (S0 * exp(lp) / E - 1.0));
-      gu[(size_t)(m - 1) * N + p + H] = (float)(pf * (S0 * exp(lm) / E - 1.0));
+      gu[(size_t)(m - 1) * N + p] = fmaxf((float)(pf * (S0 * exp(lp) / E - 1.0)), 0.f);
+      gu[(size_t)(m - 1) * N + p + H] = fmaxf((float)(pf * (S0 * exp(lm) / E - 1.0)), 0.f);
     }
   }
   std::vector<float> dtf((size_t)M + 1), edtf((size_t)M + 1);

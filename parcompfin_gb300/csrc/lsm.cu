@@ -22,8 +22,8 @@
 // Phases:
 //   forward   each thread generates its antithetic pairs (path p takes +z,
 //             path p + H takes -z, as pathsfinder pairs them) and writes the
-//             signed moneyness u(date m) = pf (S/E - 1), m = 1..M, to an FP32
-//             time-major path matrix in HBM
+//             positive part of the signed moneyness, max(pf (S/E - 1), 0) at
+//             dates m = 1..M, to an FP32 time-major path matrix in HBM
 //             (row m-1; plus half at columns [0, Hp), minus half at
 //             [Hp, 2Hp), Hp = H rounded up to 4), coalesced across the warp;
 //   backward  for m = M-1..1 the block's slice of row m-1 (two contiguous
@@ -47,8 +47,10 @@
 // exercise date (8 bits where M <= 255). The
 // regression basis is {1, u, u^2} with u = pf (S - E)/E: the reference's S - E
 // rescaled (and negated for a put), the same fitted values in exact
-// arithmetic. With u stored, a path is in the money where u > 0 and its
-// payoff is E u.
+// arithmetic. Only paths in the money enter a regression or exercise, so the
+// path matrix holds x = max(u, 0): a path is in the money where x > 0, its
+// payoff is E x, and an out-of-the-money path adds exact zeros to the sums
+// in x.
 #include <math.h>
 #include <string.h>
 
@@ -198,24 +200,23 @@ __device__ __forceinline__ void issue_row(const LsmParams& P, int r, long long p
 
 // Adds one path's terms to the regression sums of a date if the path is in
 // the money there (src/mc_amer.cpp:57-66 regresses on in-the-money paths
-// only): u = pf (S - E)/E and the cash flow discounted to time 0, y = cfd.
-// The regression target is y times the date's growth factor; the factor is
-// common to every path, so regress_date applies it once to the three y sums.
-// Paths out of the money (u <= 0) add zeros, so the loop has no divergent
-// branch.
-__device__ __forceinline__ void reg_accumulate(float u, float cfd, float (&acc)[kRegSums]) {
-  const bool itm = u > 0.f;
-  const float x = itm ? u : 0.f;
-  const float y = itm ? cfd : 0.f;
+// only): x = max(u, 0) with u = pf (S - E)/E, as the path matrix holds it,
+// and the cash flow discounted to time 0, y = cfd. The regression target is
+// y times the date's growth factor; the factor is common to every path, so
+// regress_date applies it once to the three y sums. A path out of the money
+// has x = 0, so the terms in x add exact zeros without a select; only the
+// count and the y sum test it.
+__device__ __forceinline__ void reg_accumulate(float x, float cfd, float (&acc)[kRegSums]) {
+  const bool itm = x > 0.f;
   const float x2 = x * x;
   acc[0] += itm ? 1.f : 0.f;
   acc[1] += x;
   acc[2] += x2;
   acc[3] = fmaf(x2, x, acc[3]);
   acc[4] = fmaf(x2, x2, acc[4]);
-  acc[5] += y;
-  acc[6] = fmaf(y, x, acc[6]);
-  acc[7] = fmaf(y, x2, acc[7]);
+  acc[5] += itm ? cfd : 0.f;
+  acc[6] = fmaf(cfd, x, acc[6]);
+  acc[7] = fmaf(cfd, x2, acc[7]);
 }
 
 // Reduce-scatter of eight FP32 sums over a warp: each step sends half of the
@@ -443,9 +444,11 @@ __device__ __forceinline__ void regress_date(const LsmParams& P, LsmShared<NW>& 
 }
 
 // Antithetic pair p over the contract's M dates (path p takes +z, path p + H
-// takes -z, as pathsfinder pairs them): writes the signed moneyness
-// u = pf (S/E - 1) of both paths to the path matrix, one row per date, and
-// returns u at date M of the plus and the minus path. Date m0 + l + 1 takes
+// takes -z, as pathsfinder pairs them): writes the positive part of the
+// signed moneyness, x = max(u, 0) with u = pf (S/E - 1), of both paths to the
+// path matrix, one row per date, and returns x at date M of the plus and the
+// minus path. Only x enters the sweep: a path is in the money where x > 0,
+// and its payoff is E x. Date m0 + l + 1 takes
 // lane l of Philox block m0 / 4: whole blocks first, without per-date checks,
 // then the last 1..3 dates.
 __device__ __forceinline__ float2 forward_pair(const LsmParams& P, const RngKey& key,
@@ -461,8 +464,8 @@ __device__ __forceinline__ float2 forward_pair(const LsmParams& P, const RngKey&
   auto step = [&](float z) {
     Lp += fmaf(b2, z, a2);
     Lm += fmaf(nb2, z, a2);
-    Up = fmaf(pf, ex2_approx(Lp), -pf);  // pf (S/E - 1)
-    Um = fmaf(pf, ex2_approx(Lm), -pf);
+    Up = fmaxf(fmaf(pf, ex2_approx(Lp), -pf), 0.f);  // max(pf (S/E - 1), 0)
+    Um = fmaxf(fmaf(pf, ex2_approx(Lm), -pf), 0.f);
     row[0] = Up;
     row[Hp] = Um;
     row += stride;
