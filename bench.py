@@ -89,14 +89,14 @@ def _fp32_roofline(flop_per_unit, units, ms, sms, sm_mhz):
 # DRAM bytes per algorithmic byte of the American cluster kernel, from one
 # `ncu --set full` capture of its launch on the amerbatch workload (64 puts,
 # 2^16 paths, 50 dates; dram__bytes_read.sum + dram__bytes_write.sum =
-# 1635.3 MB for 1677.7 MB algorithmic). Traffic grows with the path-dates, so
+# 1637.4 MB for 1677.7 MB algorithmic). Traffic grows with the path-dates, so
 # other launches of the kernel scale by it.
-LSM_TRAFFIC_PER_ALG_BYTE = 1635.3 / 1677.7
+LSM_TRAFFIC_PER_ALG_BYTE = 1637.4 / 1677.7
 # What bounds the American cluster kernel, from the same capture.
 LSM_LIMITER = ("the per-date regression chain, not HBM: each date is a fused pass over the "
                "CTA's paths, then one warp reduces, exchanges the sums across the cluster and "
-               "solves while the other warps wait (ncu, 64-put launch: 58 % of issue slots "
-               "busy, DRAM 32 % of peak, barrier the top stall)")
+               "solves while the other warps wait (ncu, 64-put launch: 56 % of issue slots "
+               "busy, DRAM 38 % of peak, barrier the top stall)")
 
 
 class EurWorkload:
