@@ -674,6 +674,9 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
         for (int h = 0; h < 2; ++h) {
           const int s = h * PB + 4 * j;
           float4 c = ld4(S.cf + s);
+          // Date m-1's slice is not written by this pass: load it before the
+          // exercise update's stores, so its latency overlaps the update.
+          const float4 un = NX ? ld4(nxt + s) : make_float4(0.f, 0.f, 0.f, 0.f);
           if (MD != 0) {
             const float4 u = ld4(cur + s);
             decide(u.x, c.x, s);
@@ -683,7 +686,7 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
             st4(S.cf + s, c);
           }
           if (NX) {
-            const float4 u = ld4(nxt + s);
+            const float4 u = un;
             reg_accumulate(u.x, c.x, acc);
             reg_accumulate(u.y, c.y, acc);
             reg_accumulate(u.z, c.z, acc);
