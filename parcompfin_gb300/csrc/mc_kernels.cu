@@ -75,7 +75,7 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
     for (int kk = 0; kk < 4; ++kk) {
       const long long q = q0 + (long long)(k0 + kk) * BS;
       if (k0 + kk < qpt && q < nq) {
-        const float4 z = normals4(draw_words(key, (uint64_t)(C.x0 + q), 0u));
+        const float4 z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + q), 0u));
         float s[4] = {ex2_approx(fmaf(C.b2, z.x, a2)), ex2_approx(fmaf(C.b2, z.y, a2)),
                       ex2_approx(fmaf(C.b2, z.z, a2)), ex2_approx(fmaf(C.b2, z.w, a2))};
         float y[4];
@@ -132,14 +132,14 @@ __device__ __forceinline__ void asia_path(const McContract& C, const RngKey& key
   const int M = C.M, Mfull = M & ~3;
   float L = 0.f, I = 0.f, lg = 0.f;
   for (int m0 = 0; m0 < Mfull; m0 += 4) {
-    const float4 z = normals4(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)(m0 >> 2)));
+    const float4 z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)(m0 >> 2)));
     asia_step<MODE, CV>(C, w, z.x, L, I, lg);
     asia_step<MODE, CV>(C, w, z.y, L, I, lg);
     asia_step<MODE, CV>(C, w, z.z, L, I, lg);
     asia_step<MODE, CV>(C, w, z.w, L, I, lg);
   }
   if (Mfull < M) {
-    const float4 z = normals4(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)(Mfull >> 2)));
+    const float4 z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)(Mfull >> 2)));
     asia_step<MODE, CV>(C, w, z.x, L, I, lg);
     if (Mfull + 1 < M) asia_step<MODE, CV>(C, w, z.y, L, I, lg);
     if (Mfull + 2 < M) asia_step<MODE, CV>(C, w, z.z, L, I, lg);
@@ -194,7 +194,7 @@ __device__ __forceinline__ void basket_path(const McContract& C, const float* fb
 #pragma unroll
   for (int b4 = 0; b4 < DMAX / 4; ++b4) {
     if (4 * b4 < d) {
-      const float4 z = normals4(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)b4));
+      const float4 z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)b4));
 #pragma unroll
       for (int a4 = 0; a4 < DMAX / 4; ++a4) {
         if (4 * a4 < d && (a4 >= b4 || !tri)) {
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(kTcBlock, 4) mc_basket_tc_kernel(McLaunch L) {
         for (int h = 0; h < 2; ++h) {
           const int k4 = 2 * ch + h;
           float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (4 * k4 < d) z = normals4(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)k4));
+          if (4 * k4 < d) z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)k4));
           const float4 hi = make_float4(tf32_round(z.x), tf32_round(z.y), tf32_round(z.z),
                                         tf32_round(z.w));
           const float4 lo = make_float4(tf32_round(z.x - hi.x), tf32_round(z.y - hi.y),

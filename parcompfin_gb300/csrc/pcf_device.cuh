@@ -97,6 +97,28 @@ __device__ __forceinline__ float4 normals4(uint4 w) {
                      r1 * sin_approx(t1));
 }
 
+// normals4 with the two pairs side by side in packed FP32x2 arithmetic: each
+// lane rounds exactly as the scalar operation, so the normals are the same
+// bits; the Monte Carlo kernels, issue-bound, spend fewer instructions on
+// them (the Longstaff-Schwartz forward pass, bound by HBM writes, keeps the
+// scalar form, which measured faster there).
+__device__ __forceinline__ float4 normals4_x2(uint4 w) {
+  const float kNeg2Ln2 = -1.38629436112f;
+  const float2 f = __fadd2_rn(make_float2(__uint_as_float(0x3f800000u | (w.x >> 9)),
+                                          __uint_as_float(0x3f800000u | (w.z >> 9))),
+                              make_float2(-0.99999994f, -0.99999994f));  // uniform_open
+  const float2 l = __fmul2_rn(make_float2(kNeg2Ln2, kNeg2Ln2),
+                              make_float2(lg2_approx(f.x), lg2_approx(f.y)));
+  const float2 r = make_float2(sqrt_approx(l.x), sqrt_approx(l.y));
+  const float2 t = __ffma2_rn(make_float2(3.14159265359f, 3.14159265359f),
+                              make_float2(__uint_as_float(0x40000000u | (w.y >> 9)),
+                                          __uint_as_float(0x40000000u | (w.w >> 9))),
+                              make_float2(-9.42477758f, -9.42477758f));  // bm_angle
+  const float2 c = __fmul2_rn(r, make_float2(cos_approx(t.x), cos_approx(t.y)));
+  const float2 s = __fmul2_rn(r, make_float2(sin_approx(t.x), sin_approx(t.y)));
+  return make_float4(c.x, s.x, c.y, s.y);
+}
+
 __device__ __forceinline__ float lane4(const float4& v, int l) {
   return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w));
 }
