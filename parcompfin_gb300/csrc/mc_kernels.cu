@@ -151,17 +151,71 @@ __device__ __forceinline__ void asia_path(const McContract& C, const RngKey& key
   mo.add(Y, G);
 }
 
+// asia_step for two paths side by side (lanes .x and .y) in packed FP32x2
+// arithmetic: each lane rounds exactly as the scalar step.
+template <int MODE, bool CV>
+__device__ __forceinline__ void asia_step2(const McContract& C, float2 w2, float2 z, float2& L,
+                                           float2& I, float2& lg) {
+  const float2 a2 = make_float2(C.a2, C.a2), b2 = make_float2(C.b2, C.b2);
+  if (MODE == 0) {
+    const float2 c = __ffma2_rn(make_float2(C.c2, C.c2), z, make_float2(C.c1, C.c1));
+    I = __ffma2_rn(make_float2(ex2_approx(L.x), ex2_approx(L.y)), c, I);
+    L = __fadd2_rn(L, __ffma2_rn(b2, z, a2));
+  } else {
+    L = __fadd2_rn(L, __ffma2_rn(b2, z, a2));
+    I = __fadd2_rn(I, make_float2(ex2_approx(L.x), ex2_approx(L.y)));
+  }
+  if (CV) lg = __ffma2_rn(w2, L, lg);
+}
+
+// Two Asian paths at once (asia_path for paths n0 and n1, the same bits),
+// their moments added in path order.
+template <int MODE, bool CV>
+__device__ __forceinline__ void asia_path2(const McContract& C, const RngKey& key, long long n0,
+                                           long long n1, float w, Moments<CV>& mo) {
+  const int M = C.M, Mfull = M & ~3;
+  const float2 w2 = make_float2(w, w);
+  float2 L = make_float2(0.f, 0.f), I = L, lg = L;
+  for (int m0 = 0; m0 < Mfull; m0 += 4) {
+    const float4 z0 = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n0), (uint32_t)(m0 >> 2)));
+    const float4 z1 = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n1), (uint32_t)(m0 >> 2)));
+    asia_step2<MODE, CV>(C, w2, make_float2(z0.x, z1.x), L, I, lg);
+    asia_step2<MODE, CV>(C, w2, make_float2(z0.y, z1.y), L, I, lg);
+    asia_step2<MODE, CV>(C, w2, make_float2(z0.z, z1.z), L, I, lg);
+    asia_step2<MODE, CV>(C, w2, make_float2(z0.w, z1.w), L, I, lg);
+  }
+  if (Mfull < M) {
+    const float4 z0 = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n0), (uint32_t)(Mfull >> 2)));
+    const float4 z1 = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n1), (uint32_t)(Mfull >> 2)));
+    asia_step2<MODE, CV>(C, w2, make_float2(z0.x, z1.x), L, I, lg);
+    if (Mfull + 1 < M) asia_step2<MODE, CV>(C, w2, make_float2(z0.y, z1.y), L, I, lg);
+    if (Mfull + 2 < M) asia_step2<MODE, CV>(C, w2, make_float2(z0.z, z1.z), L, I, lg);
+  }
+  if (CV && MODE == 0) lg = __ffma2_rn(make_float2(C.w_last - w, C.w_last - w), L, lg);
+  const float sw = C.S0 * w;
+  mo.add(payoff(C, I.x * sw), CV ? payoff(C, C.S0 * ex2_approx(lg.x)) : 0.f);
+  mo.add(payoff(C, I.y * sw), CV ? payoff(C, C.S0 * ex2_approx(lg.y)) : 0.f);
+}
+
 template <bool CV, int BS>
 __device__ __forceinline__ void asia_item(const McContract& C, int j, Moments<CV>& mo) {
   const RngKey key{C.seed_lo, C.seed_hi, C.stream, TAG_ASIA};
   const float w = 1.f / (float)C.M;
   const int ppt = C.units_per_item / BS;
+  // Paths k and k + 1 of the thread side by side, then the odd one out.
 #pragma unroll 1
-  for (int k = 0; k < ppt; ++k) {
+  for (int k = 0; k < ppt; k += 2) {
     const long long n = (long long)j * C.units_per_item + (long long)k * BS + threadIdx.x;
     if (n >= C.N) break;
-    if (C.mode == 0) asia_path<0, CV>(C, key, n, w, mo);
-    else asia_path<1, CV>(C, key, n, w, mo);
+    const long long n1 = n + BS;
+    if (k + 1 < ppt && n1 < C.N) {
+      if (C.mode == 0) asia_path2<0, CV>(C, key, n, n1, w, mo);
+      else asia_path2<1, CV>(C, key, n, n1, w, mo);
+    } else {
+      if (C.mode == 0) asia_path<0, CV>(C, key, n, w, mo);
+      else asia_path<1, CV>(C, key, n, w, mo);
+      break;
+    }
   }
 }
 
