@@ -76,11 +76,18 @@ __device__ __forceinline__ void eur_item(const McContract& C, int j, Moments<CV>
       const long long q = q0 + (long long)(k0 + kk) * BS;
       if (k0 + kk < qpt && q < nq) {
         const float4 z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + q), 0u));
-        float s[4] = {ex2_approx(fmaf(C.b2, z.x, a2)), ex2_approx(fmaf(C.b2, z.y, a2)),
-                      ex2_approx(fmaf(C.b2, z.z, a2)), ex2_approx(fmaf(C.b2, z.w, a2))};
-        float y[4];
-#pragma unroll
-        for (int l = 0; l < 4; ++l) y[l] = payoff(C, s[l]);
+        // Paths (0, 2) and (1, 3) side by side in packed FP32x2 arithmetic
+        // (each lane rounds exactly as the scalar operation).
+        const float2 b2 = make_float2(C.b2, C.b2), a22 = make_float2(a2, a2);
+        const float2 e02 = __ffma2_rn(b2, make_float2(z.x, z.z), a22);
+        const float2 e13 = __ffma2_rn(b2, make_float2(z.y, z.w), a22);
+        const float2 s02 = make_float2(ex2_approx(e02.x), ex2_approx(e02.y));
+        const float2 s13 = make_float2(ex2_approx(e13.x), ex2_approx(e13.y));
+        const float2 pf = make_float2(C.pf, C.pf), nK = make_float2(C.nK, C.nK);
+        const float2 v02 = __ffma2_rn(pf, s02, nK), v13 = __ffma2_rn(pf, s13, nK);
+        float s[4] = {s02.x, s13.x, s02.y, s13.y};
+        float y[4] = {fmaxf(v02.x, 0.f), fmaxf(v13.x, 0.f), fmaxf(v02.y, 0.f),
+                      fmaxf(v13.y, 0.f)};  // payoff
         if (q >= nfull) {  // the one partial quad at the end of the contract
           const long long left = C.N - 4 * q;
 #pragma unroll
@@ -242,24 +249,30 @@ __device__ __forceinline__ void basket_path(const McContract& C, const float* fb
   const float* vol = fb + DMAX;
   const float* Lf = fb + 2 * DMAX;
   const bool tri = C.mode == 0;
-  float x[DMAX];
+  // Rows 2p and 2p + 1 side by side (x2[p].x, x2[p].y) in packed FP32x2
+  // FMAs: each lane accumulates its row in the scalar order.
+  float2 x2[DMAX / 2];
 #pragma unroll
-  for (int a = 0; a < DMAX; ++a) x[a] = 0.f;
+  for (int p = 0; p < DMAX / 2; ++p) x2[p] = make_float2(0.f, 0.f);
 #pragma unroll
   for (int b4 = 0; b4 < DMAX / 4; ++b4) {
     if (4 * b4 < d) {
       const float4 z = normals4_x2(draw_words(key, (uint64_t)(C.x0 + n), (uint32_t)b4));
+      const float2 zx = make_float2(z.x, z.x), zy = make_float2(z.y, z.y);
+      const float2 zz = make_float2(z.z, z.z), zw = make_float2(z.w, z.w);
 #pragma unroll
       for (int a4 = 0; a4 < DMAX / 4; ++a4) {
         if (4 * a4 < d && (a4 >= b4 || !tri)) {
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int a = 4 * a4 + j;
-            const float4 l = *reinterpret_cast<const float4*>(Lf + a * DMAX + 4 * b4);
-            x[a] = fmaf(l.x, z.x, x[a]);
-            x[a] = fmaf(l.y, z.y, x[a]);
-            x[a] = fmaf(l.z, z.z, x[a]);
-            x[a] = fmaf(l.w, z.w, x[a]);
+          for (int h = 0; h < 2; ++h) {
+            const int p = 2 * a4 + h;  // rows 2p, 2p + 1
+            // staged as (L[2p][k], L[2p+1][k]) pairs along k
+            const float4 q0 = *reinterpret_cast<const float4*>(Lf + p * 2 * DMAX + 8 * b4);
+            const float4 q1 = *reinterpret_cast<const float4*>(Lf + p * 2 * DMAX + 8 * b4 + 4);
+            x2[p] = __ffma2_rn(make_float2(q0.x, q0.y), zx, x2[p]);
+            x2[p] = __ffma2_rn(make_float2(q0.z, q0.w), zy, x2[p]);
+            x2[p] = __ffma2_rn(make_float2(q1.x, q1.y), zz, x2[p]);
+            x2[p] = __ffma2_rn(make_float2(q1.z, q1.w), zw, x2[p]);
           }
         }
       }
@@ -267,11 +280,16 @@ __device__ __forceinline__ void basket_path(const McContract& C, const float* fb
   }
   float bsk = 0.f, geo = 0.f;
 #pragma unroll
-  for (int a = 0; a < DMAX; ++a) {
-    if (a < d) {
-      const float l2 = fmaf(vol[a], x[a], l0[a]);
-      bsk += ex2_approx(l2);
-      geo += l2;
+  for (int p = 0; p < DMAX / 2; ++p) {
+    if (2 * p < d) {
+      const float2 l2 = __ffma2_rn(*reinterpret_cast<const float2*>(vol + 2 * p), x2[p],
+                                   *reinterpret_cast<const float2*>(l0 + 2 * p));
+      bsk += ex2_approx(l2.x);
+      geo += l2.x;
+      if (2 * p + 1 < d) {
+        bsk += ex2_approx(l2.y);
+        geo += l2.y;
+      }
     }
   }
   const float inv_d = 1.f / (float)d;
@@ -367,16 +385,20 @@ mc_kernel(McLaunch L) {
       asia_item<CV, BS>(C, j, mo);
     } else {
       if (loaded != c) {  // the previous item's readers are past the final barrier
-        // Host layout [l0 (d) | v (d) | L (d x d)] -> padded [l0 | v | L rows of DMAX].
+        // Host layout [l0 (d) | v (d) | L (d x d)] -> padded [l0 | v | L]: L's
+        // rows 2p and 2p + 1 interleaved, L[2p][k] at 2 DMAX p + 2k and
+        // L[2p+1][k] next to it, zero beyond the factor.
         const int d = C.M;
         const float* src = L.basket_data + C.basket_off;
         for (int i = threadIdx.x; i < (2 + DMAX) * DMAX; i += BS) {
-          const int row = i / DMAX, col = i % DMAX;
           float v = 0.f;
-          if (row < 2) {
+          if (i < 2 * DMAX) {
+            const int row = i / DMAX, col = i % DMAX;
             if (col < d) v = src[row * d + col];
-          } else if (row - 2 < d && col < d) {
-            v = src[2 * d + (row - 2) * d + col];
+          } else {
+            const int e = i - 2 * DMAX;
+            const int row = 2 * (e / (2 * DMAX)) + (e & 1), col = (e % (2 * DMAX)) >> 1;
+            if (row < d && col < d) v = src[2 * d + row * d + col];
           }
           s_fb[i] = v;
         }
