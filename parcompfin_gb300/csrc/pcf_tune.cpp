@@ -219,7 +219,8 @@ int eur_quads_per_thread(long long N, const TuneTable& t) {
 // Asian: at least asia_steps monitoring steps per thread per work item.
 int asia_paths_per_thread(int M, const TuneTable& t) {
   const int steps = t.asia_steps[asia_class(M)];
-  return std::max(1, std::min(32, (steps + M - 1) / M));
+  const int per = std::max(1, std::min(32, (steps + M - 1) / M));
+  return per > 1 ? (per + 1) & ~1 : per;  // threads price their paths in pairs
 }
 
 bool basket_tensor(int d, const TuneTable& t) { return d > 32 || (d > 16 && d >= t.tc_min_d); }
