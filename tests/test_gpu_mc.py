@@ -109,8 +109,10 @@ def _asia_twin(orc, S0, E, r, sig, T, N, M, pf, mode, seed):
 
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("N,M", [(1, 1), (7, 3), (1000, 12), (4096, 13), (20000, 52),
-                                 (3000, 252)])
+                                 (3000, 252), (10001, 252), (257, 7)])
 def test_asia_matches_fp64_twin(orc, ctx, mode, N, M):
+    # Threads price their paths in pairs: odd N and odd paths per thread leave
+    # a path without a partner at the end of an item.
     from parcompfin_gb300 import mc_asia_result
     for pf in (1, -1):
         res = mc_asia_result(100, 100, .04, .3, 1.0, N, M, pf, mode=mode, seed=13, use_cv=True,
