@@ -653,8 +653,8 @@ __device__ void lsm_body(const LsmParams& P, int b, int rank) {
       // Exercise decision at date m (src/mc_amer.cpp:73-106) for one path:
       // exercise where the path is in the money and the payoff beats the
       // continuation value; the cash flow becomes the payoff discounted to 0.
-      auto decide = [&](float u, float& cfd, int s) {
-        float cont, ex = u * E;  // the payoff before its max with 0
+      auto decide = [&](float u, float& cfd, int s) {  // u: the stored max(u, 0)
+        float cont, ex = u * E;  // the payoff E max(u, 0)
         if (MD == 1) {
           cont = cfd * em;
         } else {
