@@ -24,8 +24,11 @@
 // Between polls the loop admits every request that has arrived into the free
 // slots, spread evenly over them (at most max_batch each), so work admitted
 // while other slots run overlaps with them on the device, and one slot's
-// host-side plan build overlaps another's kernels. Latency is arrival ->
-// result on the host, measured on the wall clock.
+// host-side plan build overlaps another's kernels. While work is on the
+// device the loop polls its slots' events without sleeping (it yields the
+// core between polls): a timed sleep of even 10 us overslept by tens of
+// microseconds and added them to every batch's latency. Latency is arrival
+// -> result on the host, measured on the wall clock.
 //
 // The loop (ServeLoop) is shared by both front ends: the trace replay feeds
 // it arrivals from the caller's thread; the live server runs it on a worker
@@ -527,7 +530,7 @@ extern "C" int pcf_serve_trace(pcf_ctx* ctx, const pcf_server_config* cfg_in, in
           if (arrival[next] - loop.now() > 200e-6)
             std::this_thread::sleep_for(std::chrono::microseconds(50));
         } else {
-          std::this_thread::sleep_for(std::chrono::microseconds(10));
+          std::this_thread::yield();  // work on the device: poll again at once
         }
       }
     }
@@ -605,13 +608,13 @@ void serve_worker_loop(pcf_server* s) {
       if (s->incoming.empty()) break;
     }
     if (!progress) {
-      std::unique_lock<std::mutex> lk(s->mu);
-      if (loop.idle())
+      if (loop.idle()) {
+        std::unique_lock<std::mutex> lk(s->mu);
         s->work_cv.wait_for(lk, std::chrono::milliseconds(5),
                             [s] { return !s->incoming.empty() || s->stop; });
-      else
-        s->work_cv.wait_for(lk, std::chrono::microseconds(10),
-                            [s] { return !s->incoming.empty(); });
+      } else {
+        std::this_thread::yield();  // work on the device: poll again at once
+      }
     }
   }
   loop.release();
