@@ -74,6 +74,25 @@ def test_american_batch_against_twin(orc, ctx, N):
             assert abs(r.sums[k] - s[k]) <= 3e-4 * abs(s[k]), (N, k, r.sums[k], s[k])
 
 
+def test_american_batch_long_and_mixed_dates_against_twin(orc, ctx):
+    """Contracts of different date counts in one cluster launch (the launch
+    sizes its shared memory for the longest), including more than 255
+    dates (16-bit exercise dates): each against the FP64 twin, and each the
+    same bits alone and in the batch."""
+    import parcompfin_gb300 as pcf
+    spec = [(100.0, .3, 300, 3), (105.0, .25, 30, 4), (95.0, .35, 61, 5), (100.0, .2, 7, 6)]
+    reqs = [pcf.request("amer", 100, E, .05, sig, 1.0, 1 << 15, "put", M=M, seed=11, stream=st)
+            for E, sig, M, st in spec]
+    out = pcf.price_batch(reqs, ctx=ctx)
+    for q, r, (E, sig, M, st) in zip(reqs, out, spec):
+        s = (C.c_double * 6)()
+        orc.twin_mc_amer(100, E, .05, sig, 1.0, 1 << 15, M, -1, 0, 11, st, s)
+        for k in (0, 2):
+            assert abs(r.sums[k] - s[k]) <= 3e-4 * abs(s[k]), (M, k, r.sums[k], s[k])
+        alone = pcf.price_batch([q], ctx=ctx)[0]
+        assert list(alone.sums) == list(r.sums), M
+
+
 def test_american_batch_against_lattice(orc, ctx):
     import parcompfin_gb300 as pcf
     reqs = [pcf.request("amer", 100, E, .05, .3, 1.0, 1 << 17, "put", M=50, use_cv=True, seed=9,
