@@ -468,7 +468,8 @@ class BinomWorkload:
 
 
 class MixedWorkload:
-    """Config 4: the served mixed stream at a fixed relative standard error."""
+    """The served mixed stream (1000 requests: European, basket, Asian and American)
+    at a fixed relative standard error."""
     name = "mixed"
     metric = ("MC paths/sec at fixed std-error (5e-4 of price), mixed request stream; "
               "p50/p99 latency served")

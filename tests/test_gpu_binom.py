@@ -44,8 +44,8 @@ def test_reference_mode_matches_reference_outputs(ctx, case):
 
 
 def test_reference_mode_random_contracts_vs_oracle(orc, ctx):
-    """Config-1 style contracts (K, r, sigma, T, call/put as specified) at
-    N the O(N^2) oracle finishes quickly; one batched launch."""
+    """Contracts drawn like the 1024-contract book (K, r, sigma, T, call/put)
+    at N the O(N^2) oracle finishes quickly; one batched launch."""
     from parcompfin_gb300 import binom_embar_batch
     rng = random.Random(7)
     cs = []
